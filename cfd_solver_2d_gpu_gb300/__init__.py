@@ -1,0 +1,295 @@
+"""GB300-native explicit finite-volume step for 2D unstructured meshes (FP64).
+
+Python mirror of the reference's per-step interface over the C ABI of
+include/fvgb.h (libfvgb.so, built in-tree by build.py):
+
+    params = Params.from_toml("input.toml")          # TomlFileManager
+    mesh = Mesh.read_su2("mesh.su2", params)          # SU2MeshReader + FVM_2D + OldDataConverter
+    solver = GPUSolver2(mesh, params)                 # GPUSolver2::allocateMemory/initializeData
+    t = solver.iteration_device(t, T)                 # CIteration::iteration_device
+    res = solver.update_residual_vector()             # GPUSolver2::updateResidualVector
+
+There is no CPU fallback: every compute call goes to the CUDA library, and
+loading fails loudly when it is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfvgb.so")
+
+__all__ = ["Params", "Mesh", "GPUSolver2", "FvgbError", "lib", "write_periodic_square", "write_cylinder",
+           "initial_field"]
+
+
+class FvgbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fvgb error {code}: {msg}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    """fvgb_params (include/fvgb.h)."""
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "equation", "flux_scheme", "reconstruct", "gradient", "limiter", "time_advance", "lsq_det_ref",
+        "wall_bc_ref", "restrict_ref", "ic_type", "renumber", "device")] + [
+        (n, ctypes.c_double) for n in ("gamma", "R", "Pr", "mu0", "T0", "CFL", "T_end", "Re")] + [
+        ("inf", ctypes.c_double * 4), ("inlet", ctypes.c_double * 4), ("outlet", ctypes.c_double * 4),
+        ("vortex", ctypes.c_double * 3), ("shock", ctypes.c_double * 4), ("mesh_scale", ctypes.c_double),
+        ("max_iteration", ctypes.c_int), ("pad_", ctypes.c_int)]
+
+    @classmethod
+    def default(cls):
+        p = cls()
+        _check(lib().fvgb_params_default(ctypes.byref(p)))
+        return p
+
+    @classmethod
+    def from_toml(cls, path):
+        p = cls()
+        name = ctypes.create_string_buffer(512)
+        _check(lib().fvgb_params_read_toml(os.fsencode(path), ctypes.byref(p), name, 512))
+        p.mesh_name = name.value.decode()
+        return p
+
+
+class MeshSoA(ctypes.Structure):
+    _fields_ = [("num_node", ctypes.c_int), ("num_element", ctypes.c_int), ("num_edge", ctypes.c_int),
+                ("num_boundary", ctypes.c_int)] + [
+        (n, ctypes.c_void_p) for n in ("node_xy", "elem_nodes", "elem_edges", "elem_neighbors", "elem_xy",
+                                       "elem_volume", "edge_nodes", "edge_L", "edge_R", "edge_setID",
+                                       "edge_periodicPair", "edge_length", "edge_distance", "edge_xy",
+                                       "edge_normal", "boundary_type")]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libfvgb.so (building it first when it is missing or stale)."""
+    global _lib
+    if _lib is None:
+        from . import build as _build
+        try:
+            _build.build()
+        except Exception as exc:  # no nvcc: use a prebuilt library if present
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"libfvgb.so is missing and cannot be built: {exc}") from exc
+        L = ctypes.CDLL(LIB_PATH)
+        i, d, v, c = ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_char_p
+        dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+        sig = {
+            "fvgb_params_default": (i, [v]),
+            "fvgb_params_read_toml": (i, [c, v, c, i]),
+            "fvgb_mesh_read_su2": (i, [c, i, d, ctypes.POINTER(v)]),
+            "fvgb_mesh_view": (i, [v, ctypes.POINTER(MeshSoA)]),
+            "fvgb_mesh_free": (None, [v]),
+            "fvgb_write_su2_periodic_square": (i, [c, i, d, d, ctypes.c_ulonglong]),
+            "fvgb_write_su2_cylinder": (i, [c, i, i, d, d, d]),
+            "fvgb_initial_field": (i, [ctypes.POINTER(MeshSoA), v, dp]),
+            "fvgb_create": (i, [ctypes.POINTER(MeshSoA), v, ctypes.POINTER(v)]),
+            "fvgb_destroy": (None, [v]),
+            "fvgb_set_state": (i, [v, dp]),
+            "fvgb_get_state": (i, [v, dp]),
+            "fvgb_step": (i, [v, dp, d, i]),
+            "fvgb_step_async": (i, [v, d, i]),
+            "fvgb_set_time": (i, [v, d]),
+            "fvgb_time": (i, [v, dp, dp]),
+            "fvgb_synchronize": (i, [v]),
+            "fvgb_rhs": (i, [v, dp, dp, dp, dp]),
+            "fvgb_dt": (i, [v, dp]),
+            "fvgb_residual": (i, [v, i, dp]),
+            "fvgb_device_status": (i, [v, ctypes.POINTER(ctypes.c_longlong)]),
+            "fvgb_device_state": (i, [v, ctypes.POINTER(v), ip]),
+            "fvgb_cell_permutation": (i, [v, ip]),
+            "fvgb_edge_permutation": (i, [v, ip]),
+            "fvgb_layout_connectivity": (i, [v, ip, ip, ip, ip]),
+            "fvgb_kernel_launches": (ctypes.c_longlong, [v]),
+            "fvgb_last_error": (c, []),
+            "fvgb_version": (c, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise FvgbError(rc, lib().fvgb_last_error().decode())
+    return rc
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) if a is not None else None
+
+
+class Mesh:
+    """Host mesh in the reference's numbering (fvgb_mesh)."""
+
+    def __init__(self, ptr):
+        self._ptr = ptr
+        self.soa = MeshSoA()
+        _check(lib().fvgb_mesh_view(self._ptr, ctypes.byref(self.soa)))
+        s = self.soa
+        self.V, self.N, self.E, self.NB = s.num_node, s.num_element, s.num_edge, s.num_boundary
+
+    @classmethod
+    def read_su2(cls, path, params=None, equation=None, scale=None):
+        eq = equation if equation is not None else (params.equation if params is not None else 1)
+        sc = scale if scale is not None else (params.mesh_scale if params is not None else 1.0)
+        ptr = ctypes.c_void_p()
+        _check(lib().fvgb_mesh_read_su2(os.fsencode(path), int(eq), float(sc), ctypes.byref(ptr)))
+        return cls(ptr)
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            lib().fvgb_mesh_free(self._ptr)
+            self._ptr = None
+
+    def array(self, name):
+        N, E, V, NB = self.N, self.E, self.V, self.NB
+        spec = {"node_xy": ("d", (2, V)), "elem_nodes": ("i", (4, N)), "elem_edges": ("i", (4, N)),
+                "elem_neighbors": ("i", (4, N)), "elem_xy": ("d", (2, N)), "elem_volume": ("d", (N,)),
+                "edge_nodes": ("i", (2, E)), "edge_L": ("i", (E,)), "edge_R": ("i", (E,)),
+                "edge_setID": ("i", (E,)), "edge_periodicPair": ("i", (E,)), "edge_length": ("d", (E,)),
+                "edge_distance": ("d", (E,)), "edge_xy": ("d", (2, E)), "edge_normal": ("d", (2, E)),
+                "boundary_type": ("i", (NB,))}
+        code, shape = spec[name]
+        ct = ctypes.c_double if code == "d" else ctypes.c_int
+        n = int(np.prod(shape))
+        ptr = ctypes.cast(getattr(self.soa, name), ctypes.POINTER(ct * n))
+        return np.frombuffer(ptr.contents, dtype=np.float64 if code == "d" else np.int32).reshape(shape).copy()
+
+
+def initial_field(mesh, params):
+    U = np.zeros((4, mesh.N))
+    _check(lib().fvgb_initial_field(ctypes.byref(mesh.soa), ctypes.byref(params), _dp(U)))
+    return U
+
+
+def write_periodic_square(path, n, L=10.0, jitter=0.0, seed=20261203):
+    _check(lib().fvgb_write_su2_periodic_square(os.fsencode(path), int(n), float(L), float(jitter), int(seed)))
+
+
+def write_cylinder(path, n_theta, n_r, r0=0.5, r1=20.0, first_dr=1e-3):
+    _check(lib().fvgb_write_su2_cylinder(os.fsencode(path), int(n_theta), int(n_r), float(r0), float(r1),
+                                          float(first_dr)))
+
+
+class GPUSolver2:
+    """One solver on one GPU (fvgb_handle); names follow GPU::GPUSolver2 and CIteration."""
+
+    def __init__(self, mesh, params):
+        self.mesh, self.params = mesh, params
+        self._h = ctypes.c_void_p()
+        _check(lib().fvgb_create(ctypes.byref(mesh.soa), ctypes.byref(params), ctypes.byref(self._h)))
+        self.N, self.E = mesh.N, mesh.E
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fvgb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    # state ---------------------------------------------------------------
+    def set_state(self, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != (4, self.N):
+            raise ValueError(f"state must have shape (4, {self.N})")
+        _check(lib().fvgb_set_state(self._h, _dp(U)))
+
+    def get_state(self, out=None):
+        U = out if out is not None else np.empty((4, self.N))
+        _check(lib().fvgb_get_state(self._h, _dp(U)))
+        return U
+
+    def set_state_ptr(self, host_ptr):
+        _check(lib().fvgb_set_state(self._h, ctypes.cast(host_ptr, ctypes.POINTER(ctypes.c_double))))
+
+    def get_state_ptr(self, host_ptr):
+        _check(lib().fvgb_get_state(self._h, ctypes.cast(host_ptr, ctypes.POINTER(ctypes.c_double))))
+
+    # stepping --------------------------------------------------------------
+    def iteration_device(self, t, T):
+        """One step of CIteration::iteration_device; returns the new time."""
+        return self.step(t, T, 1)
+
+    def step(self, t, T, nsteps):
+        tt = ctypes.c_double(t)
+        _check(lib().fvgb_step(self._h, ctypes.byref(tt), float(T), int(nsteps)))
+        return tt.value
+
+    def step_async(self, T, nsteps):
+        _check(lib().fvgb_step_async(self._h, float(T), int(nsteps)))
+
+    def set_time(self, t):
+        _check(lib().fvgb_set_time(self._h, float(t)))
+
+    def time(self):
+        t, dt = ctypes.c_double(), ctypes.c_double()
+        _check(lib().fvgb_time(self._h, ctypes.byref(t), ctypes.byref(dt)))
+        return t.value, dt.value
+
+    def synchronize(self):
+        _check(lib().fvgb_synchronize(self._h))
+
+    # parity hooks --------------------------------------------------------------
+    def rhs(self, U, gradients=False):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        R = np.empty_like(U)
+        gx = np.empty_like(U) if gradients else None
+        gy = np.empty_like(U) if gradients else None
+        _check(lib().fvgb_rhs(self._h, _dp(U), _dp(R), _dp(gx), _dp(gy)))
+        return (R, gx, gy) if gradients else R
+
+    def dt(self):
+        out = ctypes.c_double()
+        _check(lib().fvgb_dt(self._h, ctypes.byref(out)))
+        return out.value
+
+    def update_residual_vector(self, norm=0):
+        out = np.zeros(4)
+        _check(lib().fvgb_residual(self._h, int(norm), _dp(out)))
+        return out
+
+    def device_status(self):
+        out = (ctypes.c_longlong * 4)()
+        _check(lib().fvgb_device_status(self._h, out))
+        return list(out)
+
+    def device_state(self):
+        p, n = ctypes.c_void_p(), ctypes.c_int()
+        _check(lib().fvgb_device_state(self._h, ctypes.byref(p), ctypes.byref(n)))
+        return p.value, n.value
+
+    def cell_permutation(self):
+        out = np.empty(self.N, dtype=np.int32)
+        _check(lib().fvgb_cell_permutation(self._h, _ip(out)))
+        return out
+
+    def edge_permutation(self):
+        out = np.empty(self.E, dtype=np.int32)
+        _check(lib().fvgb_edge_permutation(self._h, _ip(out)))
+        return out
+
+    def layout_connectivity(self):
+        ee = np.empty((3, self.N), dtype=np.int32)
+        nb = np.empty((3, self.N), dtype=np.int32)
+        eL = np.empty(self.E, dtype=np.int32)
+        eR = np.empty(self.E, dtype=np.int32)
+        _check(lib().fvgb_layout_connectivity(self._h, _ip(ee), _ip(nb), _ip(eL), _ip(eR)))
+        return ee, nb, eL, eR
+
+    def kernel_launches(self):
+        return int(lib().fvgb_kernel_launches(self._h))

@@ -1,0 +1,113 @@
+"""Benchmark and test workloads: synthetic meshes of the named shapes and the
+input.toml text for each (same keys as the reference's input.toml,
+FVMR/src/input/TomlFileManager.cpp:110-170, plus the [gpu] table).
+
+    vortex_small   64 x 64 periodic vortex, 8,192 cells, Euler, Roe, first order, RK3, CFL 0.5
+    vortex_large   1448 x 1448 jittered vortex, 4,193,408 cells, LSQ + Barth, Roe or LLF, SSP-RK3, CFL 0.8
+    cylinder_ns    512 x 256 O-grid, 262,144 cells, Navier-Stokes, Ma 0.2, Re 100, LSQ, RK3
+    vortex_adjoint 256 x 256 jittered vortex, 131,072 cells, LSQ + Barth, Roe, SSP-RK3
+"""
+import os
+import tempfile
+
+from . import write_cylinder, write_periodic_square
+
+JITTER_SEED = 20261203
+
+
+def _num(x):
+    """A float as TOML accepts it: no leading zeros in the exponent (1.79e-5, not 1.79e-05)."""
+    s = repr(float(x))
+    if "e" in s:
+        mant, exp = s.split("e")
+        sign = "-" if exp.startswith("-") else ""
+        s = f"{mant}e{sign}{int(exp.lstrip('+-'))}"
+    return s
+
+
+def toml_text(*, equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=3103, CFL=0.5,
+              T_end=1000.0, ic_type=2, vortex=(5.0, 5.0, 5.0), inf_mode=1, inf=(1.0, 1.0, 1.0, 1.0), Ma=0.2,
+              AoA=0.0, Re=None, mu0=17.9e-6, Pr=0.72, ref_area=1.0, lsq_det="ref", wall_bc="ref", restrict="ref",
+              renumber=1, filename="mesh", max_iteration=1000):
+    lines = [
+        "[basic]", "continue = false", "dimension = 2", f'filename = "{filename}"', 'meshFileType = "su2"',
+        "useGPU = 1", "isDebugMode = false", "",
+        "[constant]", "T0 = 288.16", "p0 = 101325.0", f"Pr = {_num(Pr)}", "gamma = 1.4", f"referenceArea = {_num(ref_area)}",
+    ]
+    if Re is not None:
+        lines += [f"Re = {_num(Re)}", "calculate_mu0_by_Re = true"]
+    else:
+        lines += [f"mu0 = {_num(mu0)}", "calculate_mu0_by_Re = false"]
+    lines += ["", "[initialCondition]", f"type = {ic_type}"]
+    if ic_type == 2:
+        lines += ["[initialCondition.isentropicVortex]", f"vortex_x = {_num(vortex[0])}", f"vortex_y = {_num(vortex[1])}",
+                  f"vortex_strength = {_num(vortex[2])}"]
+    lines += ["", "[boundaryCondition.2D.inf]"]
+    if inf_mode == 1:
+        lines += ["input_mode = 1", f"rho = {_num(inf[0])}", f"u = {_num(inf[1])}", f"v = {_num(inf[2])}", f"p = {_num(inf[3])}"]
+    else:
+        lines += ["input_mode = 0", f"Ma = {_num(Ma)}", f"AoA = {_num(AoA)}"]
+    lines += ["", "[output]", "step_per_print = 50", "step_per_output_field = 100", "step_per_output_hist = 100",
+              f"maxIteration = {max_iteration}", "tolerace_residual = 1e-7", "",
+              "[physicsModel]", f"equation = {equation}", "",
+              "[time]", "is_steady = 0", "is_explicit = 1", f"CFL = {_num(CFL)}", f"max_physical_time = {_num(T_end)}",
+              f"time_advance = {time_advance}", "",
+              "[inviscid_flux_method]", f"flag_reconstruct = {reconstruct}", f"flag_gradient = {gradient}",
+              f"flux_conservation_scheme = {flux}", f"flux_limiter = {limiter}", "",
+              "[gpu]", f'lsq_det = "{lsq_det}"', f'wall_bc = "{wall_bc}"', f'restrict = "{restrict}"',
+              f"renumber = {renumber}", ""]
+    return "\n".join(lines)
+
+
+def cache_dir():
+    d = os.environ.get("FVGB_CACHE", os.path.join(tempfile.gettempdir(), "fvgb_meshes"))
+    os.makedirs(d, exist_ok=True)
+    return d
+
+
+def square_mesh(n, jitter=0.0, L=10.0, seed=JITTER_SEED, directory=None):
+    path = os.path.join(directory or cache_dir(), f"square_{n}_{jitter:g}_{seed}.su2")
+    if not os.path.exists(path):
+        tmp = path + f".{os.getpid()}.tmp"
+        write_periodic_square(tmp, n, L, jitter, seed)
+        os.replace(tmp, path)
+    return path
+
+
+def cylinder_mesh(n_theta, n_r, r0=0.5, r1=20.0, first_dr=1e-3, directory=None):
+    path = os.path.join(directory or cache_dir(), f"cyl_{n_theta}_{n_r}_{r0:g}_{r1:g}_{first_dr:g}.su2")
+    if not os.path.exists(path):
+        tmp = path + f".{os.getpid()}.tmp"
+        write_cylinder(tmp, n_theta, n_r, r0, r1, first_dr)
+        os.replace(tmp, path)
+    return path
+
+
+def write_case(directory, name, toml, mesh_path):
+    os.makedirs(directory, exist_ok=True)
+    tp = os.path.join(directory, name + ".toml")
+    with open(tp, "w") as f:
+        f.write(toml)
+    return tp, mesh_path
+
+
+def vortex_small(directory, n=64, time_advance=3103, **kw):
+    """64 x 64 periodic vortex (8,192 cells): Euler, Roe, first order, RK3, CFL 0.5."""
+    args = dict(flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=time_advance, CFL=0.5)
+    args.update(kw)
+    return write_case(directory, f"vortex_small_{n}", toml_text(**args), square_mesh(n))
+
+
+def vortex_large(directory, n=1448, flux=2002, **kw):
+    """1448 x 1448 jittered vortex (4,193,408 cells): LSQ + Barth, SSP-RK3, CFL 0.8."""
+    args = dict(flux=flux, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.8)
+    args.update(kw)
+    return write_case(directory, f"vortex_large_{n}_{flux}", toml_text(**args), square_mesh(n, jitter=0.2))
+
+
+def cylinder_ns(directory, n_theta=512, n_r=256, **kw):
+    """Laminar cylinder, Ma 0.2, Re 100 (diameter), Pr 0.72, LSQ + Barth, RK3."""
+    args = dict(equation=2, flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3103, CFL=0.5,
+                ic_type=1, inf_mode=0, Ma=0.2, AoA=0.0, Re=100.0, Pr=0.72, ref_area=1.0)
+    args.update(kw)
+    return write_case(directory, f"cylinder_ns_{n_theta}_{n_r}", toml_text(**args), cylinder_mesh(n_theta, n_r))

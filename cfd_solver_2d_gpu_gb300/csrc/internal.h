@@ -1,0 +1,59 @@
+// Shared declarations of the fvgb library (host side).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "fvgb.h"
+
+namespace fvgb {
+
+// boundary type codes, FVMR/src/global/Constexpr.h:47-57
+enum BcType : int {
+    BC_INTERIOR = -1,
+    BC_WALL_NONVISCOUS = 6001,
+    BC_WALL_ADIABAT = 6002,
+    BC_INLET = 6011,
+    BC_OUTLET = 6012,
+    BC_INF = 6013,
+    BC_DSR = 6014,
+    BC_SYMMETRY = 6021,
+    BC_PERIODIC_0 = 6100,
+    BC_PERIODIC_9 = 6109,
+};
+
+// constants of FVMR/src/math/CommonValue.h:16-29
+constexpr double kEps = 1e-10;
+constexpr double kRhoMax = 300.0;
+constexpr double kPMax = 400.0 * 101325.0;
+constexpr double kPi = 3.1415926535897;
+
+// Host mesh in the reference's numbering and [row][index] layout.
+struct HostMesh {
+    int N = 0, E = 0, V = 0, NB = 0;
+    std::vector<double> node_xy;    // 2V
+    std::vector<int> elem_nodes;    // 4N
+    std::vector<int> elem_edges;    // 4N
+    std::vector<int> elem_nbrs;     // 4N
+    std::vector<double> elem_xy;    // 2N
+    std::vector<double> elem_vol;   // N
+    std::vector<int> edge_nodes;    // 2E
+    std::vector<int> edge_L, edge_R, edge_set, edge_pair;  // E
+    std::vector<double> edge_len, edge_dist;                // E
+    std::vector<double> edge_xy, edge_normal;               // 2E
+    std::vector<int> bc_type;       // NB
+    std::vector<std::string> bc_name;
+};
+
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+
+int read_su2(const char* path, int equation, double scale, HostMesh& m);
+void mesh_view(const HostMesh& m, fvgb_mesh_soa& s);
+int initial_field(const fvgb_mesh_soa& s, const fvgb_params& p, double* U);
+
+}  // namespace fvgb
+
+struct fvgb_mesh {
+    fvgb::HostMesh m;
+};

@@ -1,0 +1,213 @@
+// Device-side physics of the explicit step, FP64.
+//
+// Each function computes what the cited reference function computes.  The
+// formulas are rearranged to spend fewer FP64 divides and square roots (the
+// FP64 pipe, not HBM, bounds this step on GB300): one reciprocal of rho per
+// state instead of three divides, one reciprocal square root for the Roe
+// average, T*sqrt(T) for T^1.5.  Results differ from the reference's by a few
+// ulp per operation; decisions (range checks, limiter bounds, far-field
+// branches) are taken on the same quantities in the same way.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fvgb {
+
+// cell state (rho, rho u, rho v, rho E): 32-byte aligned so one state is one sector
+typedef double4_32a d4;
+__host__ __device__ __forceinline__ d4 mk4(double x, double y, double z, double w) {
+    d4 r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    r.w = w;
+    return r;
+}
+
+namespace dev {
+
+constexpr double kEps = 1e-10;                  // FVMR/src/math/CommonValue.h:24
+constexpr double kRhoMax = 300.0;               // CommonValue.h:27
+constexpr double kPMax = 400.0 * 101325.0;      // CommonValue.h:30
+
+struct Gas {
+    double gamma, ga1, gam_over_ga1, inv_ga1, Etm_c, inv_gamma;  // derived constants
+    double R, Cv, Cp, inv_Cv, C1;                                 // viscous constants
+};
+
+struct Prim {
+    double r, u, v, p, ir;  // rho, u, v, p, 1/rho
+};
+
+// U2ruvp_host, FVMR/src/math/PhysicalKernel.h:11-18
+__device__ __forceinline__ Prim to_prim(const d4 U, const Gas& g) {
+    Prim w;
+    w.ir = 1.0 / U.x;
+    w.r = U.x;
+    w.u = U.y * w.ir;
+    w.v = U.z * w.ir;
+    w.p = w.r * g.ga1 * (U.w * w.ir - (w.u * w.u + w.v * w.v) * 0.5);
+    return w;
+}
+
+// ruvp2U_host, PhysicalKernel.h:20-27
+__device__ __forceinline__ d4 to_cons(double r, double u, double v, double p, const Gas& g) {
+    return mk4(r, r * u, r * v, p * g.inv_ga1 + 0.5 * r * (u * u + v * v));
+}
+
+// Restrict::outOfRange, FVMR/src/space/restrict/Restrict.h:15-23
+__device__ __forceinline__ bool out_of_range(double r, double p) {
+    return r < kEps || r > kRhoMax || p < kEps || p > kPMax;
+}
+
+// get_U_reconstruct_singleValue (linear), FVMR/src/space/Flux.cpp:28-39
+__device__ __forceinline__ d4 lin(const d4 U, const d4 gx, const d4 gy, double dx, double dy) {
+    return mk4(fma(gy.x, dy, fma(gx.x, dx, U.x)), fma(gy.y, dy, fma(gx.y, dx, U.y)),
+                        fma(gy.z, dy, fma(gx.z, dx, U.z)), fma(gy.w, dy, fma(gx.w, dx, U.w)));
+}
+
+// ConvectRoeCommon2d + RoeDissapationTerm2d, FVMR/src/space/convection/Roe.cpp:380-538
+// (entropy fix off, static mesh)
+__device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, double nx, double ny, double area,
+                                            const Gas& g) {
+    const double unL = nx * L.u + ny * L.v, unR = nx * R.u + ny * R.v;
+    const double ruL = L.r * unL, ruR = R.r * unR;
+    const double V2L = L.u * L.u + L.v * L.v, V2R = R.u * R.u + R.v * R.v;
+    const double HL = g.gam_over_ga1 * L.p * L.ir + 0.5 * V2L;
+    const double HR = g.gam_over_ga1 * R.p * R.ir + 0.5 * V2R;
+    const double psum = L.p + R.p;
+    d4 F = mk4(0.5 * (ruL + ruR), 0.5 * (fma(ruL, L.u, ruR * R.u) + nx * psum),
+                             0.5 * (fma(ruL, L.v, ruR * R.v) + ny * psum), 0.5 * fma(ruL, HL, ruR * HR));
+    // Roe averages: rm = sqrt(rR rL), rrorl = sqrt(rR/rL) = rR / rm
+    const double irm = rsqrt(R.r * L.r);
+    const double rm = (R.r * L.r) * irm;
+    const double rrorl = R.r * irm;
+    const double w = 1.0 / (rrorl + 1.0);
+    const double um = fma(R.u, rrorl, L.u) * w;
+    const double vm = fma(R.v, rrorl, L.v) * w;
+    const double Hm = fma(HR, rrorl, HL) * w;
+    const double Vm2 = um * um + vm * vm;
+    const double am2 = g.ga1 * (Hm - 0.5 * Vm2);
+    const double iam = rsqrt(am2);
+    const double am = am2 * iam;
+    const double un = um * nx + vm * ny;
+    const double eig1 = fabs(un), eig2 = fabs(un + am), eig3 = fabs(un - am);
+    const double dE = (HR - R.p * R.ir) - (HL - L.p * L.ir);
+    const double Etm = fma(g.Etm_c, Vm2, Hm * g.inv_gamma);
+    const double dW0 = R.r - L.r;
+    const double dW1 = fma(rm, R.u - L.u, dW0 * um);
+    const double dW2 = fma(rm, R.v - L.v, dW0 * vm);
+    const double dW3 = fma(rm, dE, dW0 * Etm);
+    const double astar = (eig2 + eig3) * 0.5;
+    const double Mstar = (eig2 - eig3) * 0.5 * iam;
+    const double dun = nx * (R.u - L.u) + ny * (R.v - L.v);
+    const double dp = R.p - L.p;
+    const double ae = astar - eig1;
+    const double dUroe = fma(Mstar, dun, ae * dp * irm * (iam * iam));
+    const double dProe = fma(Mstar, dp, ae * rm * dun);
+    const double dUr = dUroe * rm;
+    F.x -= 0.5 * fma(eig1, dW0, dUr);
+    F.y -= 0.5 * fma(eig1, dW1, fma(dUr, um, dProe * nx));
+    F.z -= 0.5 * fma(eig1, dW2, fma(dUr, vm, dProe * ny));
+    F.w -= 0.5 * fma(eig1, dW3, fma(dUr, Hm, dProe * un));
+    F.x *= area;
+    F.y *= area;
+    F.z *= area;
+    F.w *= area;
+    return F;
+}
+
+// LocalLaxFriedrichs, FVMR/src/space/convection/LocalLaxFriedrichs.cpp:4-47
+__device__ __forceinline__ d4 llf_flux(const d4 UL, const d4 UR, const Prim& L, const Prim& R,
+                                            double nx, double ny, double length, const Gas& g) {
+    const double unL = nx * L.u + ny * L.v, unR = nx * R.u + ny * R.v;
+    const double ruL = L.r * unL, ruR = R.r * unR;
+    const double hl = g.gam_over_ga1 * L.p * L.ir + 0.5 * (L.u * L.u + L.v * L.v);
+    const double hr = g.gam_over_ga1 * R.p * R.ir + 0.5 * (R.u * R.u + R.v * R.v);
+    const double aL = fabs(unL) + sqrt(g.gamma * L.p * L.ir);
+    const double aR = fabs(unR) + sqrt(g.gamma * R.p * R.ir);
+    const double lm = (aL > aR) ? aL : aR;
+    const double hlen = 0.5 * length;
+    return mk4(hlen * (ruL + ruR - lm * (UR.x - UL.x)),
+                        hlen * (fma(ruL, L.u, nx * L.p) + fma(ruR, R.u, nx * R.p) - lm * (UR.y - UL.y)),
+                        hlen * (fma(ruL, L.v, ny * L.p) + fma(ruR, R.v, ny * R.p) - lm * (UR.z - UL.z)),
+                        hlen * (fma(ruL, hl, ruR * hr) - lm * (UR.w - UL.w)));
+}
+
+// get_UR_wallNonViscous, FVMR/src/space/Flux.cpp:57-71
+__device__ __forceinline__ d4 ghost_slip(const d4 UL, const Prim& L, double nx, double ny) {
+    const double unL = L.u * nx + L.v * ny;
+    const double utL = L.u * ny - L.v * nx;
+    const double uxR = -unL * nx + utL * ny;
+    const double uyR = -unL * ny - utL * nx;
+    return mk4(UL.x, UL.x * uxR, UL.x * uyR, UL.w);
+}
+
+// get_UR_farField, FVMR/src/space/Flux.cpp:81-163.  fs = far-field state
+// (rho, u, v, p), fa = its sound speed, fson = p / rho^gamma of it.
+// Returns false if the boundary state is out of range (the reference exits).
+__device__ __forceinline__ bool ghost_farfield(const Prim& e, const double* fs, double fa, double fson, double nx,
+                                               double ny, const Gas& g, d4& UR) {
+    const double ae = sqrt(g.gamma * e.p * e.ir);
+    const double qnf = fs[1] * nx + fs[2] * ny;
+    const double qne = e.u * nx + e.v * ny;
+    const double rf = qnf - 2.0 * fa * g.inv_ga1;
+    const double re = qne + 2.0 * ae * g.inv_ga1;
+    const double qn = 0.5 * (re + rf);
+    const double as = g.ga1 * (re - rf) * 0.25;
+    double r0, u0, v0, p0;
+    if (qn <= -as) {
+        r0 = fs[0]; u0 = fs[1]; v0 = fs[2]; p0 = fs[3];
+    } else if (qn < as) {
+        double son, qtx, qty;
+        if (qn < 0) {  // subsonic inflow
+            son = fson;
+            qtx = fs[1] - qnf * nx;
+            qty = fs[2] - qnf * ny;
+        } else {       // subsonic outflow
+            son = e.p / pow(e.r, g.gamma);
+            qtx = e.u - qne * nx;
+            qty = e.v - qne * ny;
+        }
+        r0 = pow(as * as / son * g.inv_gamma, g.inv_ga1);
+        u0 = qtx + qn * nx;
+        v0 = qty + qn * ny;
+        p0 = as * as * r0 * g.inv_gamma;
+    } else {
+        r0 = e.r; u0 = e.u; v0 = e.v; p0 = e.p;
+    }
+    UR = to_cons(r0, u0, v0, p0, g);
+    return !out_of_range(r0, p0);
+}
+
+// viscous_flux_kernel, FVMR/src/space/viscous_flux/ViscousFlux.cpp:63-168 with the
+// helpers of ViscousFluxGPU.cu:7-124 and Sutherland's law of ViscousFluxGPU.h:26-32;
+// the Prandtl number is the reference's constant 0.72.
+__device__ __forceinline__ void viscous_flux(d4& F, const d4 U, const d4 gx, const d4 gy,
+                                             double nx, double ny, double area, const Gas& g) {
+    const double ir = 1.0 / U.x;
+    const double u = U.y * ir, v = U.z * ir, E = U.w * ir;
+    const double dudx = ir * (gx.y - u * gx.x);
+    const double dvdx = ir * (gx.z - v * gx.x);
+    const double dudy = ir * (gy.y - u * gy.x);
+    const double dvdy = ir * (gy.z - v * gy.x);
+    const double dEdx = ir * (gx.w - E * gx.x);
+    const double dEdy = ir * (gy.w - E * gy.x);
+    const double T = g.inv_Cv * (E - 0.5 * (u * u + v * v));
+    const double dTdx = (dEdx - u * dudx - v * dvdx) * g.inv_Cv;
+    const double dTdy = (dEdy - u * dudy - v * dvdy) * g.inv_Cv;
+    const double mu = g.C1 * (T * sqrt(T)) / (T + 110.4);
+    const double div = dudx + dvdy;
+    const double NMD = -2.0 / 3.0;
+    const double txx = mu * fma(NMD, div, 2.0 * dudx);
+    const double tyy = mu * fma(NMD, div, 2.0 * dvdy);
+    const double txy = mu * (dudy + dvdx);
+    const double akmu = g.Cp * (mu * (1.0 / 0.72));
+    const double Phix = fma(akmu, dTdx, fma(u, txx, v * txy));
+    const double Phiy = fma(akmu, dTdy, fma(u, txy, v * tyy));
+    F.y -= (txx * nx + txy * ny) * area;
+    F.z -= (txy * nx + tyy * ny) * area;
+    F.w -= (Phix * nx + Phiy * ny) * area;
+}
+
+}  // namespace dev
+}  // namespace fvgb

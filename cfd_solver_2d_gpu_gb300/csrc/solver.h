@@ -1,0 +1,67 @@
+// One solver instance on one GPU (solver.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "internal.h"
+#include "layout.h"
+#include "step_kernels.cuh"
+
+namespace fvgb {
+
+dev::Gas make_gas(const fvgb_params& p);
+dev::BcData make_bc(const fvgb_params& p);
+
+struct Solver {
+    static constexpr int kFlagCap = 4096;
+
+    fvgb_params p{};
+    Layout L;
+    int N = 0, E = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<void*> owned;
+    dev::Gas gas{};
+    dev::BcData bc{};
+    dev::MeshView mv{};
+    long long launches = 0, launches_per_step = 0;
+    dev::Status seen{};
+
+    // layout
+    int *d_e_L = nullptr, *d_e_R = nullptr, *d_e_bc = nullptr;
+    double* d_e_geom = nullptr;
+    int *d_c_edge = nullptr, *d_c_nbr = nullptr, *d_c_nnb = nullptr;
+    double *d_c_mvol = nullptr, *d_c_vol = nullptr, *d_c_lsq = nullptr, *d_c_vtx = nullptr;
+    double *d_c_gg = nullptr, *d_c_ginv = nullptr;
+    int* d_c_ggout = nullptr;
+    int *d_dt_ptr = nullptr, *d_dt_edge = nullptr;
+    int *d_cell_ref = nullptr, *d_cell_new = nullptr;
+    // fields
+    d4 *d_U = nullptr, *d_U0 = nullptr, *d_K1 = nullptr, *d_Gx = nullptr, *d_Gy = nullptr;
+    d4 *d_F = nullptr, *d_prim = nullptr, *d_rhs = nullptr, *d_res_part = nullptr;
+    double *d_alpha = nullptr, *d_alpha_vis = nullptr, *d_stage = nullptr, *d_res_out = nullptr;
+    int* d_flags = nullptr;
+    unsigned int* d_flag_count = nullptr;
+    dev::StepState* d_state = nullptr;
+    dev::StepState* h_state = nullptr;
+    dev::Status* d_status = nullptr;
+
+    ~Solver();
+    int init(const fvgb_mesh_soa& m, const fvgb_params& prm);
+    bool needs_gradient() const;
+    void enqueue_stage(int kind);
+    void enqueue_step();
+    int build_graph();
+    int check_status();
+    int step_async(double T, int nsteps);
+    int set_time(double t);
+    int get_time(double* t, double* dt);
+    int set_state(const double* U);
+    int get_state(double* U);
+    int rhs(const double* U, double* R, double* gx, double* gy);
+    int dt(double* out);
+    int residual(int norm, double* out);
+};
+
+}  // namespace fvgb

@@ -1,0 +1,46 @@
+// Launchers of the step kernels (step_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace fvgb {
+namespace dev {
+
+enum StageKind {
+    STAGE_RHS = 0,     // residual only
+    STAGE_EULER = 1,   // forward Euler (3101)
+    STAGE_RK3_1 = 2,   // Kutta RK3 (3103) stages
+    STAGE_RK3_2 = 3,
+    STAGE_RK3_3 = 4,
+    STAGE_SSP_1 = 5,   // SSP-RK3 (3104) stages
+    STAGE_SSP_2 = 6,
+    STAGE_SSP_3 = 7,
+};
+
+// Time and time step of one solver, kept on the device so a step needs no host sync.
+struct StepState {
+    double t, T, dt, dt6, dt_raw;
+    unsigned long long dtmin_bits;
+};
+
+void launch_prim(cudaStream_t s, const d4* U, d4* U0, d4* prim, int N, const Gas& g, bool copy);
+void launch_dt(cudaStream_t s, const d4* prim, const MeshView& m, const Gas& g, double value_1, double CFL,
+               bool ns, double* alpha, double* alpha_vis, unsigned long long* dtmin, Status* st);
+void launch_dt_final(cudaStream_t s, StepState* st, bool advance);
+void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const MeshView& m, d4* Gx, d4* Gy);
+void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, const d4* Gx,
+                 const d4* Gy, const MeshView& m, const Gas& g, const BcData& bc, d4* F, Status* st);
+void launch_update(cudaStream_t s, int kind, d4* U, const d4* U0, d4* K1, d4* rhs,
+                   const d4* F, const MeshView& m, const StepState* st, const Gas& g, int* flag_list,
+                   unsigned int* flag_count, int flag_cap, Status* status);
+void launch_restrict(cudaStream_t s, d4* U, const MeshView& m, const int* cell_ref_of_dev,
+                     const int* dev_of_cell_ref, int* flag_list, unsigned int* flag_count, int flag_cap,
+                     int restrict_ref, const Gas& g, Status* st);
+void launch_scatter_in(cudaStream_t s, const double* src, d4* U, const int* dev_of_ref, int N);
+void launch_gather_out(cudaStream_t s, const d4* U, double* dst, const int* dev_of_ref, int N);
+int residual_blocks(int N);
+void launch_residual(cudaStream_t s, const d4* R, int N, int norm, d4* part, double* out);
+
+}  // namespace dev
+}  // namespace fvgb

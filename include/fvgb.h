@@ -1,0 +1,155 @@
+/* fvgb.h -- C ABI of the GB300 explicit finite-volume step (FP64, one GPU).
+ *
+ * This library replaces the reference's per-step path of FVMR
+ * (OliveTIen/CFD_Solver_2D_GPU).  The reference has no plugin system; its
+ * boundary is internal C++ (cited per entry point below).  Conventions:
+ *   - every function returns 0 on success or a negative fvgb_status code and
+ *     never exits the process (the reference calls exit(), e.g.
+ *     FVMR/src/solvers/GPUSolver2.cpp:296-303, FVMR/src/gpu/GPUGlobalFunction.cu:18-34);
+ *   - host arrays are in the reference's numbering and its [var][index] SoA
+ *     layout (U[4][N] is 4 rows of N doubles);
+ *   - one handle = one GPU, one CUDA stream, all device memory owned by the
+ *     handle; a handle is used from one host thread at a time.
+ */
+#ifndef FVGB_H
+#define FVGB_H
+#include <stddef.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fvgb_status {
+    FVGB_OK = 0,
+    FVGB_ERR_ARG = -1,       /* invalid argument or size */
+    FVGB_ERR_IO = -2,        /* file cannot be read or written */
+    FVGB_ERR_FORMAT = -3,    /* malformed .su2 / input.toml */
+    FVGB_ERR_MESH = -4,      /* inconsistent mesh (periodic pairs, unknown boundary name, ...) */
+    FVGB_ERR_CUDA = -5,      /* CUDA runtime error (message in fvgb_last_error) */
+    FVGB_ERR_NAN = -6,       /* NaN in the state (the reference exits here: Restrict.cpp:26-29) */
+    FVGB_ERR_RANGE = -7,     /* negative rho or p in the time-step (CalculateDt.cpp:41-44) or far-field state out of range (Flux.cpp:157-160) */
+    FVGB_ERR_UNSUPPORTED = -8,/* option outside this path (e.g. double-Mach-reflection boundary) */
+    FVGB_ERR_TIMEOUT = -9,   /* a bounded device wait gave up */
+    FVGB_ERR_NO_DEVICE = -10
+} fvgb_status;
+
+/* The GlobalPara subset the step reads (FVMR/src/global/GlobalPara.cpp:4-90;
+ * keys of input.toml per FVMR/src/input/TomlFileManager.cpp:110-170) plus
+ * this library's mode switches. */
+typedef struct fvgb_params {
+    int equation;        /* physicsModel.equation: 1 Euler, 2 Navier-Stokes */
+    int flux_scheme;     /* inviscid_flux_method.flux_conservation_scheme: 2001 LLF, 2002 Roe */
+    int reconstruct;     /* inviscid_flux_method.flag_reconstruct: 3001 constant, 3002 linear */
+    int gradient;        /* inviscid_flux_method.flag_gradient: 1 least squares, 2 Green-Gauss */
+    int limiter;         /* inviscid_flux_method.flux_limiter: 0 none, 1 Barth */
+    int time_advance;    /* time.time_advance: 3101 Euler, 3103 Kutta RK3, 3104 SSP-RK3 */
+    int lsq_det_ref;     /* [gpu] lsq_det = "ref" (1) keeps MatrixKernel.h:48-49, "fixed" (0) corrects it */
+    int wall_bc_ref;     /* [gpu] wall_bc = "ref" (1) keeps Flux.cpp:73-79, "mirror" (0) mirrors the velocity */
+    int restrict_ref;    /* [gpu] restrict = "ref" (1) keeps Restrict.cpp:52, "fixed" (0) corrects it */
+    int ic_type;         /* initialCondition.type: 1 uniform, 2 isentropic vortex, 3 shock tube */
+    int renumber;        /* [gpu] renumber: 0 keep the file order, 1 Morton order of cells and edges */
+    int device;          /* CUDA device ordinal */
+    double gamma, R, Pr, mu0, T0, CFL, T_end, Re;
+    double inf[4], inlet[4], outlet[4];   /* rho, u, v, p */
+    double vortex[3];    /* x, y, strength */
+    double shock[4];     /* shock tube: x, y, normal x, normal y */
+    double mesh_scale;   /* constant.mesh_scale_factor */
+    int max_iteration;   /* output.maxIteration */
+    int pad_;
+} fvgb_params;
+
+/* Reference-order mesh arrays, mirroring GPU::NodeSoA / ElementSoA / EdgeSoA /
+ * BoundarySetMap (FVMR/src/gpu/datatype/*.h) as filled by
+ * U2NITS::OldDataConverter (FVMR/src/solvers/OldDataConverter.cpp:35-195). */
+typedef struct fvgb_mesh_soa {
+    int num_node, num_element, num_edge, num_boundary;
+    const double* node_xy;        /* [2][V] */
+    const int* elem_nodes;        /* [4][N], slot 3 = -1 */
+    const int* elem_edges;        /* [4][N], slot 3 = -1 */
+    const int* elem_neighbors;    /* [4][N], -1 = none (periodic faces too) */
+    const double* elem_xy;        /* [2][N] */
+    const double* elem_volume;    /* [N] */
+    const int* edge_nodes;        /* [2][E] */
+    const int* edge_L;            /* [E] */
+    const int* edge_R;            /* [E] (periodic: partner's L; boundary: -1) */
+    const int* edge_setID;        /* [E] 1-based boundary set, -1 interior */
+    const int* edge_periodicPair; /* [E] */
+    const double* edge_length;    /* [E] */
+    const double* edge_distance;  /* [E] */
+    const double* edge_xy;        /* [2][E] */
+    const double* edge_normal;    /* [2][E] */
+    const int* boundary_type;     /* [NB] */
+} fvgb_mesh_soa;
+
+typedef struct fvgb_mesh fvgb_mesh;     /* host mesh owned by the library */
+typedef struct fvgb_handle fvgb_handle; /* one solver on one GPU */
+typedef struct fvgb_batch fvgb_batch;   /* many solvers packed into one launch per stage */
+
+/* ---- configuration and mesh (host only; no GPU needed) ------------------ */
+
+/* Defaults of FVMR/src/global/GlobalPara.cpp:4-90. */
+int fvgb_params_default(fvgb_params* p);
+/* Reads input.toml like TomlFileManager::treeToGlobalParameter
+ * (FVMR/src/input/TomlFileManager.cpp:110-170, 200-265, mu0/Re 79-104).
+ * mesh_name receives basic.filename (may be NULL). */
+int fvgb_params_read_toml(const char* path, fvgb_params* p, char* mesh_name, int mesh_name_len);
+/* Reads and assembles an .su2 mesh with the reference's numbering
+ * (SU2MeshReader::read_mesh_and_process, FVMR/src/input/SU2MeshReader.cpp:10-251,
+ * FVM_2D::iniEdges.., FVMR/src/legacy/FVM_2D.cpp:36-198) in O(N). */
+int fvgb_mesh_read_su2(const char* path, int equation, double scale, fvgb_mesh** out);
+int fvgb_mesh_view(const fvgb_mesh* m, fvgb_mesh_soa* soa);
+void fvgb_mesh_free(fvgb_mesh* m);
+/* Synthetic .su2 writers for the benchmark meshes (no reference counterpart).
+ * Square [0,L]^2 with n x n quads, periodic markers, interior nodes jittered
+ * by U(-jitter*h, +jitter*h) from seed; O-grid around a cylinder. */
+int fvgb_write_su2_periodic_square(const char* path, int n, double L, double jitter, unsigned long long seed);
+int fvgb_write_su2_cylinder(const char* path, int n_theta, int n_r, double r0, double r1, double first_dr);
+/* Initial field (FieldInitializer, FVMR/src/input/FieldInitializer.cpp:129-222) on host. */
+int fvgb_initial_field(const fvgb_mesh_soa* mesh, const fvgb_params* p, double* U);
+
+/* ---- one solver ----------------------------------------------------------- */
+
+/* GPUSolver2::allocateMemory + initializeData (FVMR/src/solvers/GPUSolver2.cpp:54-165). */
+int fvgb_create(const fvgb_mesh_soa* mesh, const fvgb_params* p, fvgb_handle** out);
+void fvgb_destroy(fvgb_handle* h);
+/* host <-> device state, reference numbering (GPUSolver2::host_to_device /
+ * device_to_host, GPUSolver2.cpp:222-239). */
+int fvgb_set_state(fvgb_handle* h, const double* U);
+int fvgb_get_state(fvgb_handle* h, double* U);
+/* nsteps of CIteration::iteration_device (FVMR/src/time/CIteration.cpp:89-161):
+ * dt, t clamp against T, RK stages, restrict.  *t is read and updated. */
+int fvgb_step(fvgb_handle* h, double* t, double T, int nsteps);
+/* the same, asynchronously: t stays on the device; read it with fvgb_time(). */
+int fvgb_step_async(fvgb_handle* h, double T, int nsteps);
+int fvgb_set_time(fvgb_handle* h, double t);
+int fvgb_time(fvgb_handle* h, double* t, double* last_dt);
+int fvgb_synchronize(fvgb_handle* h);
+/* calculateFunctionF on a given state (FVMR/src/time/Evolve.cpp:98-112):
+ * rhs[4][N]; grad_x/grad_y[4][N] (limited gradients) may be NULL. */
+int fvgb_rhs(fvgb_handle* h, const double* U, double* rhs, double* grad_x, double* grad_y);
+/* get_global_dt_host of the current state (FVMR/src/time/CalculateDt.cpp:87-102). */
+int fvgb_dt(fvgb_handle* h, double* dt);
+/* GPUSolver2::updateResidualVector (GPUSolver2.cpp:294-296) on the right-hand
+ * side of the last stage: norm 0 = L-inf, 1 = L1, 2 = L2 (Residual.cpp:4-43). */
+int fvgb_residual(fvgb_handle* h, int norm, double out4[4]);
+/* device counters: [0] cells replaced by the positivity pass so far,
+ * [1] NaN cells seen, [2] out-of-range far-field states, [3] negative rho/p in dt. */
+int fvgb_device_status(fvgb_handle* h, long long out4[4]);
+/* raw device pointers of the state U[4][N] (this library's cell order) and
+ * the sizes, for callers that keep data on the GPU. */
+int fvgb_device_state(fvgb_handle* h, double** U_dev, int* n_cells);
+/* Cell permutation: perm[i] = this library's index of reference cell i. */
+int fvgb_cell_permutation(fvgb_handle* h, int* perm);
+int fvgb_edge_permutation(fvgb_handle* h, int* perm);
+/* Device-side layout arrays mapped back to reference numbering, for checking
+ * connectivity: elem_edges[3][N], elem_neighbors[3][N], edge_L[E], edge_R[E]. */
+int fvgb_layout_connectivity(fvgb_handle* h, int* elem_edges, int* elem_neighbors, int* edge_L, int* edge_R);
+/* Number of kernels this library launched on the handle's stream so far. */
+long long fvgb_kernel_launches(fvgb_handle* h);
+
+const char* fvgb_last_error(void);
+const char* fvgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

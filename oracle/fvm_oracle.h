@@ -1,0 +1,75 @@
+/* fvm_oracle.h -- CPU restatement of FVMR's explicit finite-volume step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the parity tests, smoke()
+ * and the CPU-baseline leg of bench.py check the CUDA path against.  The
+ * product never links it.  Each function follows the reference's CPU path
+ * operation by operation (file:line cited at each definition) and is built
+ * with -ffp-contract=off so it is IEEE-exact and gives the same bits on x86
+ * and Arm.  It is pinned against the reference itself compiled from source
+ * (oracle/ref, binaries fvmr_ref_f64/f32).
+ */
+#ifndef FVM_ORACLE_H
+#define FVM_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct om_mesh {
+    int N, E, V, NB;
+    double* node_xy;     /* [2][V] */
+    int* elem_nodes;     /* [4][N], slot 3 = -1 (triangles) */
+    int* elem_edges;     /* [4][N], slot 3 = -1 */
+    int* elem_nbrs;      /* [4][N], -1 = none (periodic faces included) */
+    double* elem_xy;     /* [2][N] */
+    double* elem_vol;    /* [N] */
+    int* edge_nodes;     /* [2][E] */
+    int* edge_L;         /* [E] */
+    int* edge_R;         /* [E], -1 on non-periodic boundaries */
+    int* edge_set;       /* [E], boundary set ID (1-based) or -1 */
+    int* edge_pair;      /* [E], periodic partner edge or -1 */
+    double* edge_len;    /* [E], rounded through float */
+    double* edge_dist;   /* [E], distance of cell centres (float arithmetic) */
+    double* edge_xy;     /* [2][E] */
+    double* edge_normal; /* [2][E] */
+    int* bc_type;        /* [NB] */
+} om_mesh;
+
+typedef struct om_params {
+    int equation;      /* 1 Euler, 2 Navier-Stokes */
+    int flux_scheme;   /* 2001 local Lax-Friedrichs, 2002 Roe */
+    int reconstruct;   /* 3001 constant, 3002 linear */
+    int gradient;      /* 1 least squares, 2 Green-Gauss */
+    int limiter;       /* 0 none, 1 Barth */
+    int time_advance;  /* 3101 forward Euler, 3103 Kutta RK3, 3104 SSP-RK3 */
+    int lsq_det_ref;   /* 1: the reference's 2x2 determinant guard; 0: corrected */
+    int wall_bc_ref;   /* 1: the reference's no-slip ghost state; 0: mirrored velocity */
+    int restrict_ref;  /* 1: the reference's neighbour-volume sum; 0: corrected */
+    int pad_;
+    double gamma, R, Pr, mu0, T0, CFL, T_end;
+    double inf[4], inlet[4], outlet[4]; /* rho, u, v, p */
+} om_params;
+
+/* Reads an .su2 file and assembles the mesh exactly as the reference does.
+ * Returns NULL and fills err on failure. */
+om_mesh* om_mesh_read_su2(const char* path, int equation, double scale, char* err, int errlen);
+void om_mesh_free(om_mesh* m);
+
+/* Initial field: ic 1 uniform (inf), 2 isentropic vortex (vortex = x, y, strength). */
+int om_init_field(const om_mesh* m, const om_params* p, int ic, const double* vortex, double* U);
+/* One residual evaluation: RHS = -(1/vol) * sum of edge fluxes; also the limited gradients. */
+int om_rhs(const om_mesh* m, const om_params* p, const double* U, double* rhs, double* gx, double* gy);
+/* Global time step of the state U (before the t-clamp). alpha may be NULL. */
+int om_dt(const om_mesh* m, const om_params* p, const double* U, double* dt, double* alpha);
+/* Positivity pass on U in place. Returns the number of cells replaced, -1 on NaN. */
+int om_restrict(const om_mesh* m, const om_params* p, double* U);
+/* nsteps steps of time_advance from time *t; U in place; dts[nsteps] may be NULL. */
+int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* t, double* dts, double* last_rhs);
+/* Residual norm of an RHS field: norm 0 = L-infinity, 1 = L1, 2 = L2 (per variable). */
+void om_residual(const om_mesh* m, const double* rhs, int norm, double* out4);
+/* Freestream (rho,u,v,p) from Mach and angle of attack (degrees). */
+void om_ruvp_from_mach(double Ma, double aoa_deg, double T0, double p0, double gamma, double R, double* ruvp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
