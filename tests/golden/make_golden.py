@@ -1,0 +1,121 @@
+"""Generates the golden fixtures under tests/golden/ by running the reference
+itself: the reference's CPU step path compiled from its own sources with
+myfloat = double (oracle/ref, binary oracle/_ref/fvmr_ref_f64).
+
+Run here, where the reference sources are present:
+    make -C oracle/ref && python tests/golden/make_golden.py
+
+Each fixture is one compressed .npz with the case's input.toml text, the mesh
+(.su2 text, compressed), the reference's mesh arrays, its initial field, one
+residual evaluation (rhs, limited gradients, dt) and the state after a few
+steps.  Test infrastructure.
+"""
+import gzip
+import io
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from cfd_solver_2d_gpu_gb300 import cases  # noqa: E402
+from fvmrdump import read_dump  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "fvmr_ref_f64")
+REF32 = os.path.join(ROOT, "oracle", "_ref", "fvmr_ref_f32")
+
+MESH_KEYS = ["node_xy", "elem_nodes", "elem_edges", "elem_nbrs", "elem_xy", "elem_vol", "edge_nodes", "edge_L",
+             "edge_R", "edge_set", "edge_pair", "edge_len", "edge_xy", "edge_normal", "bc_type", "U0"]
+
+
+def golden_cases(d):
+    """(name, toml text, su2 path, stepping mode, steps) of every fixture."""
+    sq16 = cases.square_mesh(16, directory=d)
+    sq24j = cases.square_mesh(24, jitter=0.2, directory=d)
+    sq64 = cases.square_mesh(64, directory=d)
+    cyl = cases.cylinder_mesh(32, 16, directory=d)
+    T = cases.toml_text
+    return [
+        # the small plain config: 64x64 vortex, Roe, first order, Kutta RK3, CFL 0.5, 1000 steps
+        ("vortex64_roe_o1_rk3", T(flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=3103, CFL=0.5),
+         sq64, "rk3", 1000),
+        ("vortex16_roe_o1_euler", T(flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=3101, CFL=0.5),
+         sq16, "euler", 20),
+        ("vortex16_llf_o1_rk3", T(flux=2001, reconstruct=3001, gradient=1, limiter=1, time_advance=3103, CFL=0.5),
+         sq16, "rk3", 20),
+        # second order on a jittered mesh: LSQ (reference determinant guard) + Barth, SSP-RK3
+        ("jvortex24_roe_lsq_barth_ssp", T(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104,
+                                          CFL=0.8), sq24j, "ssprk3", 10),
+        ("jvortex24_llf_lsq_barth_ssp", T(flux=2001, reconstruct=3002, gradient=1, limiter=1, time_advance=3104,
+                                          CFL=0.8), sq24j, "ssprk3", 10),
+        ("jvortex24_roe_gg_barth_euler", T(flux=2002, reconstruct=3002, gradient=2, limiter=1, time_advance=3101,
+                                           CFL=0.8), sq24j, "euler", 10),
+        ("jvortex24_roe_lsq_nolim_euler", T(flux=2002, reconstruct=3002, gradient=1, limiter=0, time_advance=3101,
+                                            CFL=0.2), sq24j, "euler", 3),
+        # laminar cylinder: no-slip wall, far field, Sutherland, Kutta RK3
+        ("cylinder32_ns_lsq_barth_rk3", T(equation=2, flux=2002, reconstruct=3002, gradient=1, limiter=1,
+                                          time_advance=3103, CFL=0.5, ic_type=1, inf_mode=0, Ma=0.2, Re=100.0),
+         cyl, "rk3", 5),
+        # inviscid cylinder: slip wall, far field
+        ("cylinder32_euler_roe_lsq_rk3", T(equation=1, flux=2002, reconstruct=3002, gradient=1, limiter=1,
+                                           time_advance=3103, CFL=0.5, ic_type=1, inf_mode=0, Ma=0.5), cyl, "rk3", 5),
+    ]
+
+
+def run_ref(binary, toml_path, su2, mode, steps, out):
+    r = subprocess.run([binary, toml_path, su2, mode, str(steps), out], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{binary} {mode} failed: {r.stderr[-400:]}")
+    return read_dump(out)
+
+
+def main():
+    if not os.path.exists(REF):
+        sys.exit("build the reference first: make -C oracle/ref")
+    with tempfile.TemporaryDirectory() as d:
+        for name, toml, su2, mode, steps in golden_cases(d):
+            tp = os.path.join(d, name + ".toml")
+            with open(tp, "w") as f:
+                f.write(toml)
+            rhs = run_ref(REF, tp, su2, "rhs", 0, os.path.join(d, name + "_rhs.bin"))
+            stp = run_ref(REF, tp, su2, mode, steps, os.path.join(d, name + "_step.bin"))
+            out = {k: rhs[k] for k in MESH_KEYS}
+            out.update(rhs=rhs["rhs"], grad_x=rhs["grad_x"], grad_y=rhs["grad_y"], dt=rhs["dt"],
+                       U=stp["U"], dts=stp["dts"], t=stp["t"], steps=np.array([steps]),
+                       toml=np.frombuffer(toml.encode(), dtype=np.uint8),
+                       su2_gz=np.frombuffer(gzip.compress(open(su2, "rb").read(), mtime=0), dtype=np.uint8),
+                       mode=np.frombuffer(mode.encode(), dtype=np.uint8))
+            if os.path.exists(REF32):  # the reference as shipped (float), for the record
+                s32 = run_ref(REF32, tp, su2, mode, steps, os.path.join(d, name + "_f32.bin"))
+                out["U_f32"] = s32["U"]
+            path = os.path.join(HERE, name + ".npz")
+            np.savez_compressed(path, **out)
+            print(f"{path}: N={rhs['sizes'][0]} {mode} x{steps} ({os.path.getsize(path) // 1024} KiB)")
+
+
+def load(name):
+    """Loads a fixture and materialises its input.toml and .su2 in a temp directory."""
+    z = np.load(os.path.join(HERE, name + ".npz"))
+    d = tempfile.mkdtemp(prefix="fvgb_golden_")
+    tp, sp = os.path.join(d, name + ".toml"), os.path.join(d, name + ".su2")
+    with open(tp, "wb") as f:
+        f.write(z["toml"].tobytes())
+    with open(sp, "wb") as f:
+        f.write(gzip.decompress(z["su2_gz"].tobytes()))
+    data = {k: z[k] for k in z.files}
+    data["mode"] = z["mode"].tobytes().decode()
+    return tp, sp, data
+
+
+def names():
+    return sorted(f[:-4] for f in os.listdir(HERE) if f.endswith(".npz"))
+
+
+if __name__ == "__main__":
+    main()

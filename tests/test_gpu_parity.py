@@ -1,0 +1,178 @@
+"""Parity of the CUDA path (through the C ABI) with the reference: against the
+golden fixtures the reference produced, against the oracle on the same inputs
+at larger sizes, and through size-independent properties at full size.
+
+Tolerances are relative L-infinity norms, ||a - b||_inf / ||b||_inf, in FP64:
+  residual, gradients, dt of one evaluation     1e-12
+  state after <= 20 steps                       1e-12
+  state after 1000 steps (64x64 vortex)         1e-9
+  second-order limited runs (<= 10 steps)       1e-10
+"""
+import numpy as np
+import pytest
+
+import cfd_solver_2d_gpu_gb300 as fv
+from cfd_solver_2d_gpu_gb300 import cases
+from golden import make_golden
+from oracle.pyoracle import Oracle
+
+pytestmark = pytest.mark.gpu
+NAMES = make_golden.names()
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def make(tp, sp, renumber=1):
+    p = fv.Params.from_toml(tp)
+    p.renumber = renumber
+    m = fv.Mesh.read_su2(sp, p)
+    return fv.GPUSolver2(m, p), p, m
+
+
+@pytest.fixture(scope="module", params=NAMES)
+def golden(request):
+    return request.param, make_golden.load(request.param)
+
+
+def test_residual_matches_reference(golden):
+    name, (tp, sp, g) = golden
+    s, p, m = make(tp, sp)
+    R, gx, gy = s.rhs(g["U0"], gradients=True)
+    assert rel(R, g["rhs"]) <= 1e-12, name
+    if p.reconstruct == 3002 or p.equation == 2:
+        assert rel(gx, g["grad_x"]) <= 1e-12 and rel(gy, g["grad_y"]) <= 1e-12, name
+    s.set_state(g["U0"])
+    assert abs(s.dt() - g["dt"][0]) <= 1e-12 * g["dt"][0], name
+
+
+def test_steps_match_reference(golden):
+    name, (tp, sp, g) = golden
+    s, p, m = make(tp, sp)
+    s.set_state(g["U0"])
+    n = int(g["steps"][0])
+    t = s.step(0.0, p.T_end, n)
+    U = s.get_state()
+    tol = 1e-9 if n >= 1000 else (1e-10 if p.reconstruct == 3002 else 1e-12)
+    assert rel(U, g["U"]) <= tol, (name, rel(U, g["U"]))
+    assert abs(t - g["t"][0]) <= 1e-11 * g["t"][0]
+
+
+def test_connectivity_maps_back_bit_exact(golden):
+    name, (tp, sp, g) = golden
+    s, p, m = make(tp, sp, renumber=1)
+    ee, nb, eL, eR = s.layout_connectivity()
+    N = m.N
+    ref_ee = g["elem_edges"].reshape(4, N)[:3]
+    ref_nb = g["elem_nbrs"].reshape(4, N)[:3]
+    assert np.array_equal(ee, ref_ee)
+    compact = np.full_like(ref_nb, -1)  # the device keeps valid neighbours first, in slot order
+    for c in range(N):
+        v = ref_nb[:, c][ref_nb[:, c] >= 0]
+        compact[: len(v), c] = v
+    assert np.array_equal(nb, compact)
+    assert np.array_equal(eL, g["edge_L"]) and np.array_equal(eR, g["edge_R"])
+    perm = s.cell_permutation()
+    assert np.array_equal(np.sort(perm), np.arange(N))
+
+
+def test_renumbering_does_not_change_the_answer():
+    tp, sp, g = make_golden.load("jvortex24_roe_lsq_barth_ssp")
+    a, p, _ = make(tp, sp, renumber=0)
+    b, _, _ = make(tp, sp, renumber=1)
+    for s in (a, b):
+        s.set_state(g["U0"])
+        s.step(0.0, p.T_end, 5)
+    assert rel(a.get_state(), b.get_state()) <= 1e-12
+
+
+def test_deterministic_bitwise():
+    tp, sp, g = make_golden.load("cylinder32_ns_lsq_barth_rk3")
+    s, p, _ = make(tp, sp)
+    out = []
+    for _ in range(2):
+        s.set_state(g["U0"])
+        s.step(0.0, p.T_end, 5)
+        out.append(s.get_state())
+    assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.8),
+    dict(flux=2001, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.8),
+    dict(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.8, lsq_det="fixed"),
+    dict(flux=2002, reconstruct=3002, gradient=2, limiter=1, time_advance=3103, CFL=0.8),
+])
+def test_against_oracle_128(tmp_path, cfg):
+    """128x128 jittered vortex (32,768 cells): oracle and CUDA path on the same inputs."""
+    su2 = cases.square_mesh(128, jitter=0.2, directory=str(tmp_path))
+    tp = tmp_path / "c.toml"
+    tp.write_text(cases.toml_text(**cfg))
+    o = Oracle(str(tp), su2)
+    s, p, _ = make(str(tp), su2)
+    U0 = o.init_field()
+    R, gx, _ = o.rhs(U0)
+    Rg, gxg, _ = s.rhs(U0, gradients=True)
+    assert rel(Rg, R) <= 1e-12 and rel(gxg, gx) <= 1e-12
+    U, t, _, _ = o.run(U0, 3)
+    s.set_state(U0)
+    s.step(0.0, p.T_end, 3)
+    assert rel(s.get_state(), U) <= 1e-10
+
+
+def test_against_oracle_cylinder_ns(tmp_path):
+    tp, su2 = cases.cylinder_ns(str(tmp_path), 128, 64)
+    o = Oracle(tp, su2)
+    s, p, _ = make(tp, su2)
+    U0 = o.init_field()
+    assert rel(s.rhs(U0), o.rhs(U0)[0]) <= 1e-12
+    U, t, _, _ = o.run(U0, 3)
+    s.set_state(U0)
+    s.step(0.0, p.T_end, 3)
+    assert rel(s.get_state(), U) <= 1e-11
+
+
+def test_positivity_pass_matches_oracle(tmp_path):
+    """A cell whose density is out of range is replaced by the neighbour mean, as the reference does."""
+    tp, sp, g = make_golden.load("vortex16_roe_o1_euler")
+    o = Oracle(tp, sp)
+    s, p, m = make(tp, sp)
+    U0 = g["U0"].copy()
+    U0[:, 100] = [1e-12, 0.0, 0.0, 1.0]   # rho below RHO_MIN
+    U0[:, 101] = [500.0, 0.0, 0.0, 1e3]   # rho above RHO_MAX, a neighbour of 100
+    U, _, _, _ = o.run(U0, 1)
+    s.set_state(U0)
+    s.step(0.0, p.T_end, 1)
+    assert rel(s.get_state(), U) <= 1e-12
+    assert s.device_status()[0] >= 1
+
+
+def test_nan_is_an_error_code_not_a_crash():
+    tp, sp, g = make_golden.load("vortex16_roe_o1_euler")
+    s, p, _ = make(tp, sp)
+    U0 = g["U0"].copy()
+    U0[0, 7] = np.nan
+    s.set_state(U0)
+    with pytest.raises(fv.FvgbError) as e:
+        s.step(0.0, p.T_end, 1)
+    assert e.value.code == -6
+    s.set_state(g["U0"])  # the handle stays usable
+    s.step(0.0, p.T_end, 1)
+
+
+def test_large_mesh_properties(tmp_path):
+    """1448x1448 jittered vortex (4,193,408 cells), second order, SSP-RK3: total mass
+    and energy are conserved on the periodic domain and the residual is finite."""
+    tp, su2 = cases.vortex_large(str(tmp_path))
+    s, p, m = make(tp, su2)
+    vol = m.array("elem_volume")
+    U0 = s.get_state()
+    mass0 = np.dot(vol, U0[0])
+    s.step(0.0, p.T_end, 3)
+    U = s.get_state()
+    assert np.all(np.isfinite(U))
+    assert abs(np.dot(vol, U[0]) - mass0) <= 1e-12 * mass0
+    assert abs(np.dot(vol, U[3]) - np.dot(vol, U0[3])) <= 1e-12 * np.dot(vol, U0[3])
+    res = s.update_residual_vector()
+    assert np.all(np.isfinite(res)) and res[0] > 0

@@ -1,0 +1,123 @@
+"""Host side of the library (no GPU needed): the C ABI exports, input.toml
+reading, .su2 reading and assembly against the reference's arrays, the
+initial field, the synthetic mesh writers and the error paths."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cfd_solver_2d_gpu_gb300 as fv
+from cfd_solver_2d_gpu_gb300 import cases
+from golden import make_golden
+from oracle.pyoracle import params_from_toml
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+MESH = {"node_xy": "node_xy", "elem_nodes": "elem_nodes", "elem_edges": "elem_edges",
+        "elem_neighbors": "elem_nbrs", "elem_xy": "elem_xy", "elem_volume": "elem_vol", "edge_nodes": "edge_nodes",
+        "edge_L": "edge_L", "edge_R": "edge_R", "edge_setID": "edge_set", "edge_periodicPair": "edge_pair",
+        "edge_length": "edge_len", "edge_xy": "edge_xy", "edge_normal": "edge_normal", "boundary_type": "bc_type"}
+
+
+def declared_symbols():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            names |= set(re.findall(r"\b(fvgb_\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    L = fv.lib()
+    missing = [n for n in declared_symbols() if not hasattr(L, n)]
+    assert not missing, missing
+    assert fv.lib().fvgb_version().decode().startswith("fvgb")
+
+
+@pytest.mark.parametrize("name", make_golden.names())
+def test_mesh_matches_reference(name):
+    tp, sp, g = make_golden.load(name)
+    p = fv.Params.from_toml(tp)
+    m = fv.Mesh.read_su2(sp, p)
+    for k, v in MESH.items():
+        a = m.array(k)
+        assert np.array_equal(a, g[v].reshape(a.shape)), f"{name}: {k}"
+    U0 = fv.initial_field(m, p)
+    assert np.max(np.abs(U0 - g["U0"])) <= 1e-15 * np.max(np.abs(g["U0"]))
+
+
+@pytest.mark.parametrize("name", make_golden.names())
+def test_toml_matches_reference_semantics(name):
+    tp, _, _ = make_golden.load(name)
+    p = fv.Params.from_toml(tp)
+    q, info = params_from_toml(tp)
+    for k in ("equation", "flux_scheme", "reconstruct", "gradient", "limiter", "time_advance"):
+        assert getattr(p, k) == getattr(q, k), k
+    for k in ("gamma", "R", "Pr", "mu0", "T0", "CFL", "T_end"):
+        assert getattr(p, k) == pytest.approx(getattr(q, k), rel=1e-15), k
+    assert np.allclose(list(p.inf), list(q.inf), rtol=1e-15, atol=0)
+
+
+REF_TOML = "/root/reference/quick_start/U2NITS-10.0"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TOML), reason="reference tree not mounted")
+@pytest.mark.parametrize("case", ["2D_isentropic_vortex", "2D_cylinder", "1D_shocktube"])
+def test_reads_the_references_own_input_toml(case):
+    p = fv.Params.from_toml(os.path.join(REF_TOML, case, "input.toml"))
+    assert p.mesh_name
+    assert p.flux_scheme in (2001, 2002) and p.time_advance in (3101, 3103)
+
+
+def test_su2_writers(tmp_path):
+    sq = str(tmp_path / "sq.su2")
+    fv.write_periodic_square(sq, 8, 10.0, 0.2, 7)
+    m = fv.Mesh.read_su2(sq)
+    assert (m.N, m.E, m.V) == (128, (3 * 128 + 32) // 2, 81)  # E = (3N + boundary edges) / 2
+    # periodic edges all have a partner whose partner is the edge itself
+    pair = m.array("edge_periodicPair")
+    ids = np.nonzero(pair >= 0)[0]
+    assert len(ids) == 32 and np.array_equal(pair[pair[ids]], ids)
+    # jitter stays inside +-0.2 h and boundary nodes are not moved
+    xy = m.array("node_xy")
+    h = 10.0 / 8
+    gx, gy = np.meshgrid(np.arange(9) * h, np.arange(9) * h)
+    assert np.max(np.abs(xy[0] - gx.ravel())) <= 0.2 * h + 1e-12
+    onb = (gx.ravel() == 0) | (gx.ravel() == 10) | (gy.ravel() == 0) | (gy.ravel() == 10)
+    assert np.all(xy[0][onb] == gx.ravel()[onb])
+    cy = str(tmp_path / "cy.su2")
+    fv.write_cylinder(cy, 16, 4)
+    m = fv.Mesh.read_su2(cy, equation=2)
+    assert m.N == 128 and sorted(m.array("boundary_type")) == [6002, 6013]
+    r = np.hypot(*m.array("node_xy"))
+    assert np.isclose(r.min(), 0.5) and np.isclose(r.max(), 20.0)
+
+
+def test_errors_are_codes_not_exits(tmp_path):
+    bad = tmp_path / "bad.su2"
+    bad.write_text("NDIME= 3\n")
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Mesh.read_su2(str(bad))
+    assert e.value.code == -3
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Mesh.read_su2(str(tmp_path / "missing.su2"))
+    assert e.value.code == -2
+    odd = tmp_path / "odd.su2"  # a periodic marker without its pair
+    odd.write_text("NDIME= 2\nNELEM= 1\n5 0 1 2 0\nNPOIN= 3\n0 0 0\n1 0 1\n0 1 2\nNMARK= 1\n"
+                   "MARKER_TAG= periodic_1\nMARKER_ELEMS= 1\n3 0 1\n")
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Mesh.read_su2(str(odd))
+    assert e.value.code == -4
+    t = tmp_path / "x.toml"
+    t.write_text("[constant]\ngamma = 1.4\n")
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Params.from_toml(str(t))
+    assert "missing" in str(e.value)
+
+
+def test_cases_write_valid_toml(tmp_path):
+    tp, sp = cases.vortex_small(str(tmp_path), n=8)
+    p = fv.Params.from_toml(tp)
+    assert (p.time_advance, p.reconstruct, p.CFL) == (3103, 3001, 0.5)

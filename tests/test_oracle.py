@@ -1,0 +1,100 @@
+"""The oracle (oracle/fvm_oracle.c) against the golden fixtures made by the
+reference itself (tests/golden/make_golden.py), and, where the reference was
+compiled here (oracle/_ref), against live reference runs.  CPU only."""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from golden import make_golden
+from oracle.pyoracle import Oracle
+
+NAMES = make_golden.names()
+MESH = {"node_xy": "node_xy", "elem_nodes": "elem_nodes", "elem_edges": "elem_edges", "elem_nbrs": "elem_nbrs",
+        "elem_xy": "elem_xy", "elem_vol": "elem_vol", "edge_nodes": "edge_nodes", "edge_L": "edge_L",
+        "edge_R": "edge_R", "edge_set": "edge_set", "edge_pair": "edge_pair", "edge_len": "edge_len",
+        "edge_xy": "edge_xy", "edge_normal": "edge_normal", "bc_type": "bc_type"}
+MODE_CODE = {"euler": 3101, "rk3": 3103, "ssprk3": 3104}
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module", params=NAMES)
+def case(request):
+    tp, sp, g = make_golden.load(request.param)
+    return request.param, Oracle(tp, sp), g
+
+
+def test_mesh_bit_exact(case):
+    name, o, g = case
+    for k, v in MESH.items():
+        a = o.array(v)
+        assert np.array_equal(a, g[k].reshape(a.shape)), f"{name}: {k} differs from the reference"
+
+
+def test_initial_field(case):
+    name, o, g = case
+    # exp/pow of the platform's libm: equal on x86, within a few ulp elsewhere
+    assert rel(o.init_field(), g["U0"]) <= 1e-15
+
+
+def test_residual_gradient_dt(case):
+    name, o, g = case
+    R, gx, gy = o.rhs(g["U0"])
+    assert rel(R, g["rhs"]) <= 1e-14, name
+    assert rel(gx, g["grad_x"]) <= 1e-14 and rel(gy, g["grad_y"]) <= 1e-14, name
+    dt, _ = o.dt(g["U0"])
+    assert abs(dt - g["dt"][0]) <= 1e-15 * g["dt"][0]
+
+
+def test_steps(case):
+    name, o, g = case
+    if int(g["steps"][0]) > 100:
+        pytest.skip("long run covered by the GPU parity test")
+    o.params.time_advance = MODE_CODE[g["mode"]]
+    U, t, dts, _ = o.run(g["U0"], int(g["steps"][0]))
+    assert rel(U, g["U"]) <= 1e-13, name
+    assert abs(t - g["t"][0]) <= 1e-14 * abs(g["t"][0])
+
+
+def test_bit_exact_on_x86(case):
+    """On the machine the fixtures were made on, the oracle is the reference bit for bit."""
+    import platform
+    if platform.machine() not in ("x86_64", "AMD64"):
+        pytest.skip("libm differs across architectures")
+    name, o, g = case
+    R, gx, gy = o.rhs(g["U0"])
+    assert np.array_equal(R, g["rhs"]) and np.array_equal(gx, g["grad_x"]), name
+
+
+def test_planted_mistake_is_caught():
+    """A checker that cannot fail checks nothing: plant a change in the oracle's
+    parameters (gamma 1.4 -> 1.4 + 1e-9) and the residual no longer matches."""
+    tp, sp, g = make_golden.load("jvortex24_roe_lsq_barth_ssp")
+    o = Oracle(tp, sp)
+    o.params.gamma = 1.4 + 1e-9
+    R, _, _ = o.rhs(g["U0"])
+    assert rel(R, g["rhs"]) > 1e-12
+
+
+REF = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "fvmr_ref_f64")
+
+
+@pytest.mark.skipif(not os.path.exists(REF), reason="reference not compiled here (oracle/_ref)")
+def test_live_reference_larger_mesh(tmp_path):
+    """A 96x96 jittered second-order case run by the reference binary and the oracle."""
+    from cfd_solver_2d_gpu_gb300 import cases
+    from fvmrdump import read_dump
+    su2 = cases.square_mesh(96, jitter=0.2, directory=str(tmp_path))
+    tp = tmp_path / "c.toml"
+    tp.write_text(cases.toml_text(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.8))
+    out = tmp_path / "r.bin"
+    subprocess.run([REF, str(tp), su2, "ssprk3", "3", str(out)], check=True, capture_output=True)
+    ref = read_dump(str(out))
+    o = Oracle(str(tp), su2)
+    U, t, _, _ = o.run(o.init_field(), 3)
+    assert np.array_equal(U, ref["U"])
