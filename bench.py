@@ -1,0 +1,321 @@
+#!/usr/bin/env python
+"""Throughput of the explicit finite-volume step on one GB300, FP64.
+
+Workload (the large plain configuration): 1448 x 1448 periodic square split
+into 4,193,408 triangles, interior nodes jittered by U(-0.2h, 0.2h) from seed
+20261203, isentropic vortex (strength 5 at (5,5), freestream rho=u=v=p=1),
+second order with least-squares gradients (the reference's determinant guard)
+and the Barth limiter, Roe flux (--flux llf for local Lax-Friedrichs), SSP-RK3,
+CFL 0.8.  Synthetic data of the configuration's shape; no public dataset.
+
+A "step" is one SSP-RK3 step (3 stages) of the whole mesh; the metric is
+cell-stage updates per second = cells x 3 x steps / time.  Every array of the
+step is larger than the 129 MB L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--flux roe|llf]
+
+Multi-GPU: the path is single-GPU; with N > 1 every rank runs an independent
+replica of the workload (weak scaling, no collective on the data path) and the
+time is the maximum over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_SIDE = 1448
+JSON_METRIC = "cell-stage updates/s (1 GB300, FP64, matched ref)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--flux", choices=["roe", "llf"], default="roe")
+    ap.add_argument("--n", type=int, default=N_SIDE, help="cells per side of the square (default 1448)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def workload(args, directory):
+    from cfd_solver_2d_gpu_gb300 import cases
+    flux = 2002 if args.flux == "roe" else 2001
+    tp, su2 = cases.vortex_large(directory, n=args.n, flux=flux)
+    return tp, su2, flux
+
+
+def config(args, N, E, V):
+    return {"workload": f"jittered periodic vortex {args.n}x{args.n} quads -> {N} triangles, second order "
+                        f"(LSQ + Barth), {args.flux.upper()} flux, SSP-RK3, CFL 0.8",
+            "cells": N, "edges": E, "nodes": V, "stages_per_step": 3,
+            "gradient": "least squares (reference determinant guard) + Barth", "flux": args.flux,
+            "integrator": "SSP-RK3", "l2_flush": "none needed: every per-step array exceeds the 129 MB L2",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def algorithmic_bytes(N, E, V):
+    """Bytes each kernel group must move per launch under the convention 'every
+    array element touched once, neighbour re-reads free' (FP64 8 B, int32 4 B)."""
+    return {
+        # U 32, 3 neighbour ids 12, count 4, least-squares weights 48, vertex offsets 48; grad write 64
+        "gradient": 208 * N,
+        # per edge: L,R 8, geometry 64, flux write 32; per cell: U + gradients read once 96
+        "flux": 104 * E + 96 * N,
+        # per cell: edge refs 12, -1/vol 8, U read+write 64, U0 32; per edge: flux read once 32
+        "update": 116 * N + 32 * E,
+        # prim: U 32 + prim 32 (+U0 copy 32); alpha: ids 8 + geometry 32 + prim 32/cell + alpha 8;
+        # dt cell: CSR ids + alpha + vol
+        "dt": 96 * N + 48 * E + 32 * N + 8 * N + 4 * (N + 2 * E),
+        "restrict": 8,
+    }
+
+
+def stage_bytes(N, E, V):
+    """Per-stage algorithmic bytes of the second-order step, 332 N + 48 E + 16 V."""
+    return 332 * N + 48 * E + 16 * V
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_figures(flux):
+    """Per-launch DRAM traffic and FP64 instruction counts from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_step_kernels.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(flux, {})
+    except Exception:
+        return {}
+
+
+def cpu_baseline(tp, su2, N, threads, max_steps, budget_s=30.0):
+    """The oracle's restatement of the reference step on the host, same workload, bounded sample."""
+    from oracle import pyoracle
+    used = pyoracle.set_threads(threads)
+    o = pyoracle.Oracle(tp, su2)
+    U = o.init_field()
+    t = 0.0
+    done, elapsed = 0, 0.0
+    while done < max_steps and (done == 0 or elapsed < budget_s):
+        t0 = time.perf_counter()
+        U, t, _, _ = o.run(U, 1, t)
+        elapsed += time.perf_counter() - t0
+        done += 1
+    return {"value": 3.0 * N * done / elapsed, "unit": "cell-stage updates/s", "cores": used, "kind": "port",
+            "sample": f"{done} SSP-RK3 step(s) of the full {N}-cell mesh in {elapsed:.1f} s, {used} thread(s)"}
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the reference step's CPU restatement (oracle/fvm_oracle.c) with all host threads."""
+    if rank != 0:
+        return
+    ncores = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as d:
+        tp, su2, flux = workload(args, d)
+        from oracle import pyoracle
+        pyoracle.set_threads(ncores)
+        o = pyoracle.Oracle(tp, su2)
+        N, E, V = o.N, o.E, o.V
+        U = o.init_field()
+        t = 0.0
+        for _ in range(min(args.warmup, 1)):
+            U, t, _, _ = o.run(U, 1, t)
+        steps = max(1, min(args.steps, 10))
+        t0 = time.perf_counter()
+        U, t, _, _ = o.run(U, steps, t)
+        el = time.perf_counter() - t0
+    value = 3.0 * N * steps / el
+    line = {"impl": "reference", "metric": JSON_METRIC, "value": value, "unit": "cell-stage updates/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * el / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(args, N, E, V),
+            "cpu_baseline": {"value": value, "unit": "cell-stage updates/s", "cores": ncores, "kind": "port",
+                             "sample": f"{steps} SSP-RK3 steps of the full {N}-cell mesh, {ncores} threads "
+                                       f"(the reference has no GPU path for this configuration)"},
+            "e2e": {"value": value, "unit": "cell-stage updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import cfd_solver_2d_gpu_gb300 as fv
+
+    with tempfile.TemporaryDirectory() as d:
+        tp, su2, flux = workload(args, d)
+        p = fv.Params.from_toml(tp)
+        p.device = local
+        mesh = fv.Mesh.read_su2(su2, p)
+        N, E, V = mesh.N, mesh.E, mesh.V
+        s = fv.GPUSolver2(mesh, p)
+        U0 = s.get_state()
+        T = p.T_end
+        s.set_time(0.0)
+        # warm-up
+        s.step_timed(T, args.warmup)
+
+        def barrier():
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            s.synchronize()
+
+        barrier()
+        l0 = s.kernel_launches()
+        with ClockSampler(local) as clk:
+            ms = s.step_timed(T, args.steps)
+        barrier()
+        launches = s.kernel_launches() - l0
+        if world > 1:
+            tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            ms = float(tt.item())
+        clocks = clk.summary()
+        value = 3.0 * N * args.steps * world / (ms / 1e3)
+
+        # per-kernel-group device times (same steps, launched one by one with events)
+        prof = s.profile_steps(T, max(3, min(args.steps, 20)))
+        algo = algorithmic_bytes(N, E, V)
+        dom = max((k for k in prof if prof[k][1] > 0 and k != "restrict"), key=lambda k: prof[k][0])
+        avg_ms = prof[dom][0] / prof[dom][1]
+        peak, peak_kind = measured_peaks()
+        achieved = algo[dom] / (avg_ms / 1e3) / 1e9
+        ncu = ncu_figures(args.flux)
+        traffic = ncu.get(dom, {}).get("dram_bytes_per_launch")
+        stage_ms = (prof["gradient"][0] + prof["flux"][0] + prof["update"][0]) / max(prof["update"][1], 1)
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": algo[dom], "avg_launch_ms": avg_ms,
+                "share_of_step": prof[dom][0] / sum(v[0] for v in prof.values())}
+        fp64_peak = 1207.0  # GFLOP/s, FP64 FMA chain measured on this machine's GB300 (profiles/fp64_peak.txt)
+        fp64 = None
+        if ncu.get(dom, {}).get("fp64_flop_per_launch"):
+            a64 = ncu[dom]["fp64_flop_per_launch"] / (avg_ms / 1e3) / 1e9
+            fp64 = {"achieved_gflops": a64, "peak_gflops": fp64_peak, "frac": a64 / fp64_peak,
+                    "kernel": dom, "source": "fp64 flop per launch from ncu x live launch time"}
+        stage_roof = {"achieved": stage_bytes(N, E, V) / (stage_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                      "frac": stage_bytes(N, E, V) / (stage_ms / 1e3) / 1e9 / peak,
+                      "bytes_per_stage": stage_bytes(N, E, V), "formula": "332N + 48E + 16V"}
+
+        # end to end through the C ABI with host buffers: H2D of the state, one step, D2H of the state
+        e2e = None
+        if not args.no_e2e:
+            host = torch.empty((4, N), dtype=torch.float64, pin_memory=True)
+            host.copy_(torch.from_numpy(U0))
+            k_e2e = max(3, min(args.steps, 20))
+            t = 0.0
+            s.set_state_ptr(host.data_ptr())
+            t = s.step(t, T, 1)
+            s.get_state_ptr(host.data_ptr())
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(k_e2e):
+                s.set_state_ptr(host.data_ptr())
+                t = s.step(t, T, 1)
+                s.get_state_ptr(host.data_ptr())
+            barrier()
+            el = time.perf_counter() - t0
+            e2e = {"value": 3.0 * N * k_e2e * world / el, "unit": "cell-stage updates/s",
+                   "h2d_bytes_per_step": 32 * N, "d2h_bytes_per_step": 32 * N, "steps": k_e2e,
+                   "api": "fvgb_set_state + fvgb_step + fvgb_get_state (pinned host buffers)"}
+
+        cpu = None
+        if rank == 0 and not args.no_cpu_baseline:
+            cpu = cpu_baseline(tp, su2, N, threads=1, max_steps=3)
+
+    if rank == 0:
+        line = {"metric": JSON_METRIC, "value": value, "unit": "cell-stage updates/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (generated mesh and initial field of the configuration's shape)",
+                "config": config(args, N, E, V), "clocks": clocks, "gpu_launches": launches,
+                "roofline": roof, "roofline_stage": stage_roof, "fp64": fp64, "kernel_ms": prof,
+                "e2e": e2e, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

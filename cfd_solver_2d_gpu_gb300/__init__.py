@@ -107,6 +107,8 @@ def lib():
             "fvgb_edge_permutation": (i, [v, ip]),
             "fvgb_layout_connectivity": (i, [v, ip, ip, ip, ip]),
             "fvgb_kernel_launches": (ctypes.c_longlong, [v]),
+            "fvgb_profile_steps": (i, [v, d, i, dp, ip]),
+            "fvgb_step_timed": (i, [v, d, i, dp]),
             "fvgb_last_error": (c, []),
             "fvgb_version": (c, []),
         }
@@ -293,3 +295,18 @@ class GPUSolver2:
 
     def kernel_launches(self):
         return int(lib().fvgb_kernel_launches(self._h))
+
+    def step_timed(self, T, nsteps):
+        """nsteps bracketed by CUDA events on the solver's stream; returns device milliseconds."""
+        ms = ctypes.c_double()
+        _check(lib().fvgb_step_timed(self._h, float(T), int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    PROFILE_GROUPS = ("dt", "gradient", "flux", "update", "restrict")
+
+    def profile_steps(self, T, nsteps):
+        """Per kernel group: (total ms, number of timed launches) over nsteps run without the graph."""
+        ms = np.zeros(5)
+        cnt = np.zeros(5, dtype=np.int32)
+        _check(lib().fvgb_profile_steps(self._h, float(T), int(nsteps), _dp(ms), _ip(cnt)))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.PROFILE_GROUPS)}

@@ -198,18 +198,37 @@ Solver::~Solver() {
 
 bool Solver::needs_gradient() const { return p.reconstruct == 3002 || p.equation == 2; }
 
+// event pair around one group of launches (profiling entry point only; never captured)
+void Solver::mark(int cls, bool begin) {
+    if (!prof) return;
+    cudaEvent_t ev;
+    cudaEventCreate(&ev);
+    cudaEventRecord(ev, stream);
+    if (begin) {
+        prof->open[cls] = ev;
+    } else {
+        prof->pairs.push_back({cls, prof->open[cls], ev});
+    }
+}
+
 // the residual of one stage: gradient + limiter, edge fluxes, gather + update
 void Solver::enqueue_stage(int kind) {
     cudaStream_t s = stream;
     if (needs_gradient()) {
+        mark(PROF_GRAD, true);
         dev::launch_grad(s, p.gradient, p.limiter == 1, d_U, mv, d_Gx, d_Gy);
+        mark(PROF_GRAD, false);
         launches += 1;
     }
+    mark(PROF_FLUX, true);
     dev::launch_flux(s, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv, gas, bc, d_F,
                      d_status);
+    mark(PROF_FLUX, false);
     launches += (mv.E_int > 0) + (mv.E > mv.E_int);
+    mark(PROF_UPDATE, true);
     dev::launch_update(s, kind, d_U, d_U0, d_K1, d_rhs, d_F, mv, d_state, gas, d_flags, d_flag_count, kFlagCap,
                        d_status);
+    mark(PROF_UPDATE, false);
     launches += 1;
 }
 
@@ -217,11 +236,13 @@ void Solver::enqueue_stage(int kind) {
 void Solver::enqueue_step() {
     cudaStream_t s = stream;
     const bool copy = p.time_advance != 3101;
+    mark(PROF_DT, true);
     dev::launch_prim(s, d_U, d_U0, d_prim, N, gas, copy);
     const double value_1 = std::max(4.0 / 3.0, p.gamma / p.Pr);
     dev::launch_dt(s, d_prim, mv, gas, value_1, p.CFL, p.equation == 2, d_alpha, d_alpha_vis, &d_state->dtmin_bits,
                    d_status);
     dev::launch_dt_final(s, d_state, true);
+    mark(PROF_DT, false);
     launches += 4;
     if (p.time_advance == 3101) {
         enqueue_stage(dev::STAGE_EULER);
@@ -234,9 +255,36 @@ void Solver::enqueue_step() {
         enqueue_stage(dev::STAGE_SSP_2);
         enqueue_stage(dev::STAGE_SSP_3);
     }
+    mark(PROF_RESTRICT, true);
     dev::launch_restrict(s, d_U, mv, d_cell_ref, d_cell_new, d_flags, d_flag_count, kFlagCap, p.restrict_ref, gas,
                          d_status);
+    mark(PROF_RESTRICT, false);
     launches += 1;
+}
+
+// nsteps run launch by launch (no graph) with CUDA events around each kernel
+// group on the solver's stream; returns the summed milliseconds per group
+int Solver::profile_steps(double T, int nsteps, double* ms, int* count) {
+    CK(cudaMemcpyAsync(&d_state->T, &T, sizeof(double), cudaMemcpyHostToDevice, stream));
+    Prof pr;
+    prof = &pr;
+    for (int i = 0; i < nsteps; i++) enqueue_step();
+    prof = nullptr;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
+    for (int c = 0; c < PROF_NCLASS; c++) {
+        ms[c] = 0.0;
+        count[c] = 0;
+    }
+    for (auto& q : pr.pairs) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, q.a, q.b);
+        ms[q.cls] += t;
+        count[q.cls] += 1;
+        cudaEventDestroy(q.a);
+        cudaEventDestroy(q.b);
+    }
+    return check_status();
 }
 
 int Solver::build_graph() {
@@ -522,6 +570,35 @@ extern "C" int fvgb_layout_connectivity(fvgb_handle* h, int* elem_edges, int* el
 }
 
 extern "C" long long fvgb_kernel_launches(fvgb_handle* h) { return h ? h->s.launches : -1; }
+
+extern "C" int fvgb_step_timed(fvgb_handle* h, double T, int nsteps, double* ms_out) {
+    GUARD(h);
+    if (!ms_out || nsteps < 0) return fail(FVGB_ERR_ARG, "bad timing arguments");
+    Solver& s = h->s;
+    int rc = s.build_graph();
+    if (rc) return rc;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaStreamSynchronize(s.stream));
+    CK(cudaEventRecord(a, s.stream));
+    rc = s.step_async(T, nsteps);
+    CK(cudaEventRecord(b, s.stream));
+    CK(cudaEventSynchronize(b));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms_out = ms;
+    if (rc) return rc;
+    return s.check_status();
+}
+
+extern "C" int fvgb_profile_steps(fvgb_handle* h, double T, int nsteps, double ms_out[5], int count_out[5]) {
+    GUARD(h);
+    if (!ms_out || !count_out || nsteps < 0) return fail(FVGB_ERR_ARG, "bad profiling arguments");
+    return h->s.profile_steps(T, nsteps, ms_out, count_out);
+}
 
 extern "C" const char* fvgb_last_error(void) { return g_error.c_str(); }
 

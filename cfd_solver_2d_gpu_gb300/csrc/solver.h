@@ -47,8 +47,19 @@ struct Solver {
     dev::StepState* h_state = nullptr;
     dev::Status* d_status = nullptr;
 
+    // kernel groups timed by profile_steps()
+    enum { PROF_DT = 0, PROF_GRAD = 1, PROF_FLUX = 2, PROF_UPDATE = 3, PROF_RESTRICT = 4, PROF_NCLASS = 5 };
+    struct Prof {
+        struct Pair { int cls; cudaEvent_t a, b; };
+        cudaEvent_t open[PROF_NCLASS] = {};
+        std::vector<Pair> pairs;
+    };
+    Prof* prof = nullptr;
+
     ~Solver();
     int init(const fvgb_mesh_soa& m, const fvgb_params& prm);
+    void mark(int cls, bool begin);
+    int profile_steps(double T, int nsteps, double* ms, int* count);
     bool needs_gradient() const;
     void enqueue_stage(int kind);
     void enqueue_step();

@@ -141,10 +141,22 @@ int fvgb_device_state(fvgb_handle* h, double** U_dev, int* n_cells);
 int fvgb_cell_permutation(fvgb_handle* h, int* perm);
 int fvgb_edge_permutation(fvgb_handle* h, int* perm);
 /* Device-side layout arrays mapped back to reference numbering, for checking
- * connectivity: elem_edges[3][N], elem_neighbors[3][N], edge_L[E], edge_R[E]. */
+ * connectivity: elem_edges[3][N] (slot order), elem_neighbors[3][N] (the
+ * valid face neighbours in slot order, then -1, as the gradient reads them),
+ * edge_L[E], edge_R[E]. */
 int fvgb_layout_connectivity(fvgb_handle* h, int* elem_edges, int* elem_neighbors, int* edge_L, int* edge_R);
 /* Number of kernels this library launched on the handle's stream so far. */
 long long fvgb_kernel_launches(fvgb_handle* h);
+/* nsteps of fvgb_step_async bracketed by CUDA events on the handle's stream;
+ * *ms_out = the device time between them.  t stays on the device. */
+int fvgb_step_timed(fvgb_handle* h, double T, int nsteps, double* ms_out);
+/* Runs nsteps like fvgb_step_async but launch by launch, with CUDA events on
+ * the handle's stream around each kernel group; returns the summed time (ms)
+ * and the number of timed groups for: [0] time step (4 kernels), [1] gradient
+ * + limiter, [2] edge fluxes (interior + boundary), [3] gather + stage update,
+ * [4] positivity pass.  (The reference times only whole iterations with
+ * std::chrono, FVMR/src/drivers/CDriver.cpp:73-85.) */
+int fvgb_profile_steps(fvgb_handle* h, double T, int nsteps, double ms_out[5], int count_out[5]);
 
 const char* fvgb_last_error(void);
 const char* fvgb_version(void);

@@ -12,6 +12,9 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 /* FVMR/src/math/CommonValue.h:16-29 */
 #define OM_PI 3.1415926535897
@@ -530,10 +533,16 @@ int om_init_field(const om_mesh* m, const om_params* p, int ic, const double* vo
  * matrix helpers of FVMR/src/math/MatrixKernel.h:21-93 */
 static int grad_lsq(const om_mesh* m, const om_params* p, const double* U, double* gx, double* gy) {
     const int N = m->N;
+    int bad = 0;
+#pragma omp parallel for schedule(static)
     for (int e = 0; e < N; e++) {
         int nb[3], nvn = 0;
         for (int j = 0; j < 3; j++) if (m->elem_nbrs[j * N + e] != -1) nb[nvn++] = m->elem_nbrs[j * N + e];
-        if (nvn <= 0) return -3;
+        if (nvn <= 0) {
+#pragma omp critical
+            bad = 1;
+            continue;
+        }
         double dX[6], dU[12], dXt[6], A[4], B[6], G[8];
         for (int k = 0; k < nvn; k++) {
             dX[k * 2 + 0] = m->elem_xy[nb[k]] - m->elem_xy[e];
@@ -568,12 +577,13 @@ static int grad_lsq(const om_mesh* m, const om_params* p, const double* U, doubl
         }
         for (int v = 0; v < 4; v++) { gx[v * N + e] = G[v]; gy[v * N + e] = G[4 + v]; }
     }
-    return 0;
+    return bad ? -3 : 0;
 }
 
 /* GradientGreenGauss_2, FVMR/src/space/gradient/Gradient.cpp:248-458 */
 static void grad_gg(const om_mesh* m, const double* U, double* gx, double* gy) {
     const int N = m->N, E = m->E;
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < N; c++) {
         double volC = m->elem_vol[c];
         int eid[4], etype[4], sign[4], out[4];
@@ -643,6 +653,7 @@ static void grad_gg(const om_mesh* m, const double* U, double* gx, double* gy) {
 /* LimiterBarth, FVMR/src/space/gradient/Gradient.cpp:58-114 */
 static void limiter_barth(const om_mesh* m, const double* U, double* gx, double* gy) {
     const int N = m->N, V = m->V;
+#pragma omp parallel for schedule(static)
     for (int e = 0; e < N; e++) {
         int nb[3], nvn = 0;
         for (int j = 0; j < 3; j++) if (m->elem_nbrs[j * N + e] != -1) nb[nvn++] = m->elem_nbrs[j * N + e];
@@ -941,16 +952,25 @@ int om_rhs(const om_mesh* m, const om_params* p, const double* U, double* rhs, d
     /* calculateFluxHost, Flux.cpp:394-412 */
     {
         double C1 = sutherland_C1(p);
+        int erc = 0;
+#pragma omp parallel for schedule(static)
         for (int ei = 0; ei < E; ei++) {
             double F[4];
-            rc = edge_flux(m, p, U, gx, gy, ei, F);
-            if (rc) goto done;
+            int r = edge_flux(m, p, U, gx, gy, ei, F);
+            if (r) {
+#pragma omp critical
+                erc = r;
+                continue;
+            }
             if (p->equation == 2) viscous_flux(m, p, U, gx, gy, ei, C1, F);
             for (int v = 0; v < 4; v++) ef[v * E + ei] = F[v];
         }
+        rc = erc;
+        if (rc) goto done;
     }
     /* add_edge_flux_to_element_flux, Flux.cpp:346-392, then the -1/vol scaling of
      * calculateFunctionF, FVMR/src/time/Evolve.cpp:106-111 */
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < N; c++) {
         double acc[4] = {0, 0, 0, 0};
         for (int i = 0; i < 4; i++) {
@@ -977,6 +997,7 @@ int om_dt(const om_mesh* m, const om_params* p, const double* U, double* dt_out,
     double* rv = (double*)malloc((size_t)4 * N * sizeof(double));
     double* aC = alpha_out ? alpha_out : (double*)malloc((size_t)N * sizeof(double));
     int rc = 0;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < N; i++) {
         rv[i] = U[i];
         rv[N + i] = U[N + i] / U[i];
@@ -1073,21 +1094,28 @@ int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* 
         memcpy(U0, U, M * sizeof(double));
         if (p->time_advance == 3101) { /* evolve_explicit_globaltimestep, Evolve.cpp:12-23 */
             if ((rc = om_rhs(m, p, U0, k1, NULL, NULL))) break;
+            #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) U[i] = U0[i] + dt * k1[i];
         } else if (p->time_advance == 3103) { /* Kutta RK3 with the weights of Evolve.cpp:58-86 */
             if ((rc = om_rhs(m, p, U0, k1, NULL, NULL))) break;
+            #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) Us[i] = U0[i] + 0.5 * dt * k1[i];
             if ((rc = om_rhs(m, p, Us, k2, NULL, NULL))) break;
+            #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) Us[i] = U0[i] - dt * k1[i] + 2.0 * dt * k2[i];
             if ((rc = om_rhs(m, p, Us, k3, NULL, NULL))) break;
             const double dt_on_6 = dt / 6.0;
+            #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) U[i] = U0[i] + dt_on_6 * (k1[i] + 4 * k2[i] + k3[i]);
         } else if (p->time_advance == 3104) { /* SSP-RK3 (Shu-Osher), new in this path */
             if ((rc = om_rhs(m, p, U0, k1, NULL, NULL))) break;
+            #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) U1[i] = U0[i] + dt * k1[i];
             if ((rc = om_rhs(m, p, U1, k2, NULL, NULL))) break;
+            #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) Us[i] = 0.75 * U0[i] + 0.25 * (U1[i] + dt * k2[i]);
             if ((rc = om_rhs(m, p, Us, k3, NULL, NULL))) break;
+            #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) U[i] = (1.0 / 3.0) * U0[i] + (2.0 / 3.0) * (Us[i] + dt * k3[i]);
         } else {
             rc = -2;
@@ -1105,6 +1133,16 @@ int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* 
 }
 
 /* get_residual_host, FVMR/src/output/residual/Residual.cpp:4-43 */
+int om_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
 void om_residual(const om_mesh* m, const double* rhs, int norm, double* out) {
     const int N = m->N;
     for (int v = 0; v < 4; v++) {

@@ -66,6 +66,10 @@ int om_restrict(const om_mesh* m, const om_params* p, double* U);
 int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* t, double* dts, double* last_rhs);
 /* Residual norm of an RHS field: norm 0 = L-infinity, 1 = L1, 2 = L2 (per variable). */
 void om_residual(const om_mesh* m, const double* rhs, int norm, double* out4);
+/* Host threads for the per-cell and per-edge loops (results do not depend on
+ * the count: every output value is computed by one thread in the reference's
+ * order).  n <= 0 keeps the current count; returns the count in use. */
+int om_set_threads(int n);
 /* Freestream (rho,u,v,p) from Mach and angle of attack (degrees). */
 void om_ruvp_from_mach(double Ma, double aoa_deg, double T0, double p0, double gamma, double R, double* ruvp);
 

@@ -61,8 +61,16 @@ def lib():
         L.om_run.argtypes = [ctypes.POINTER(OmMesh), ctypes.POINTER(OmParams), dp, ctypes.c_int, dp, dp, dp]
         L.om_residual.argtypes = [ctypes.POINTER(OmMesh), dp, ctypes.c_int, dp]
         L.om_ruvp_from_mach.argtypes = [ctypes.c_double] * 6 + [dp]
+        L.om_set_threads.argtypes = [ctypes.c_int]
+        L.om_set_threads.restype = ctypes.c_int
+        L.om_set_threads(int(os.environ.get("FVM_ORACLE_THREADS", "1")))
         _lib = L
     return _lib
+
+
+def set_threads(n):
+    """Host threads of the oracle's loops; returns the count in use."""
+    return lib().om_set_threads(int(n))
 
 
 def _dp(a):
