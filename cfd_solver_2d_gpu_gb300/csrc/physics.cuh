@@ -38,10 +38,45 @@ struct Prim {
     double r, u, v, p, ir;  // rho, u, v, p, 1/rho
 };
 
+// ---- comparisons on the integer pipe ------------------------------------
+// A GB300 SM issues 2 FP64 lane-operations per clock but 64 integer ones, so
+// comparisons, minima and maxima of doubles are done on their bit patterns.
+// okey() maps a double to an int64 whose signed order is the order of the
+// doubles (for non-NaN values, with -0 just below +0); min/max select one of
+// their arguments, so their results are exact.
+__device__ __forceinline__ long long okey(double x) {
+    const long long b = __double_as_longlong(x);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool dlt(double a, double b) { return okey(a) < okey(b); }
+__device__ __forceinline__ double dmax(double a, double b) { return okey(a) < okey(b) ? b : a; }
+__device__ __forceinline__ double dmin(double a, double b) { return okey(b) < okey(a) ? b : a; }
+// x > 0 and x < 0 in the IEEE sense (both false for -0 and +0)
+__device__ __forceinline__ bool pos(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool neg(double x) {
+    const long long b = __double_as_longlong(x);
+    return b < 0 && (b << 1) != 0;
+}
+__device__ __forceinline__ bool is_nan(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+
+// 1/x: the hardware's approximate reciprocal refined by two Newton steps
+// (y <- y + y (1 - x y); each step squares the relative error), within ~1 ulp
+// of the correctly rounded value for normal x.
+__device__ __forceinline__ double rcp(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
 // U2ruvp_host, FVMR/src/math/PhysicalKernel.h:11-18
 __device__ __forceinline__ Prim to_prim(const d4 U, const Gas& g) {
     Prim w;
-    w.ir = 1.0 / U.x;
+    w.ir = rcp(U.x);
     w.r = U.x;
     w.u = U.y * w.ir;
     w.v = U.z * w.ir;
@@ -54,9 +89,13 @@ __device__ __forceinline__ d4 to_cons(double r, double u, double v, double p, co
     return mk4(r, r * u, r * v, p * g.inv_ga1 + 0.5 * r * (u * u + v * v));
 }
 
-// Restrict::outOfRange, FVMR/src/space/restrict/Restrict.h:15-23
+// Restrict::outOfRange, FVMR/src/space/restrict/Restrict.h:15-23: rho or p
+// below 1e-10 or above 300 / 400 atm (NaN counts as in range, as in the
+// reference, where every comparison with NaN is false)
 __device__ __forceinline__ bool out_of_range(double r, double p) {
-    return r < kEps || r > kRhoMax || p < kEps || p > kPMax;
+    const long long kr = okey(r), kp = okey(p);
+    const bool r_nan = is_nan(r), p_nan = is_nan(p);
+    return (!r_nan && (kr < okey(kEps) || kr > okey(kRhoMax))) || (!p_nan && (kp < okey(kEps) || kp > okey(kPMax)));
 }
 
 // get_U_reconstruct_singleValue (linear), FVMR/src/space/Flux.cpp:28-39
@@ -72,16 +111,18 @@ __device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, double nx, 
     const double unL = nx * L.u + ny * L.v, unR = nx * R.u + ny * R.v;
     const double ruL = L.r * unL, ruR = R.r * unR;
     const double V2L = L.u * L.u + L.v * L.v, V2R = R.u * R.u + R.v * R.v;
-    const double HL = g.gam_over_ga1 * L.p * L.ir + 0.5 * V2L;
-    const double HR = g.gam_over_ga1 * R.p * R.ir + 0.5 * V2R;
+    const double EL = L.p * L.ir, ER = R.p * R.ir;  // p/rho
+    const double HL = fma(g.gam_over_ga1, EL, 0.5 * V2L);
+    const double HR = fma(g.gam_over_ga1, ER, 0.5 * V2R);
     const double psum = L.p + R.p;
-    d4 F = mk4(0.5 * (ruL + ruR), 0.5 * (fma(ruL, L.u, ruR * R.u) + nx * psum),
-                             0.5 * (fma(ruL, L.v, ruR * R.v) + ny * psum), 0.5 * fma(ruL, HL, ruR * HR));
+    // central part 0.5 (F_L + F_R).n, scaled by 0.5 area at the end
+    d4 F = mk4(ruL + ruR, fma(ruL, L.u, fma(ruR, R.u, nx * psum)), fma(ruL, L.v, fma(ruR, R.v, ny * psum)),
+               fma(ruL, HL, ruR * HR));
     // Roe averages: rm = sqrt(rR rL), rrorl = sqrt(rR/rL) = rR / rm
     const double irm = rsqrt(R.r * L.r);
     const double rm = (R.r * L.r) * irm;
     const double rrorl = R.r * irm;
-    const double w = 1.0 / (rrorl + 1.0);
+    const double w = rcp(rrorl + 1.0);
     const double um = fma(R.u, rrorl, L.u) * w;
     const double vm = fma(R.v, rrorl, L.v) * w;
     const double Hm = fma(HR, rrorl, HL) * w;
@@ -91,28 +132,26 @@ __device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, double nx, 
     const double am = am2 * iam;
     const double un = um * nx + vm * ny;
     const double eig1 = fabs(un), eig2 = fabs(un + am), eig3 = fabs(un - am);
-    const double dE = (HR - R.p * R.ir) - (HL - L.p * L.ir);
+    const double dE = (HR - ER) - (HL - EL);
     const double Etm = fma(g.Etm_c, Vm2, Hm * g.inv_gamma);
     const double dW0 = R.r - L.r;
-    const double dW1 = fma(rm, R.u - L.u, dW0 * um);
-    const double dW2 = fma(rm, R.v - L.v, dW0 * vm);
+    const double du = R.u - L.u, dv = R.v - L.v;
+    const double dW1 = fma(rm, du, dW0 * um);
+    const double dW2 = fma(rm, dv, dW0 * vm);
     const double dW3 = fma(rm, dE, dW0 * Etm);
     const double astar = (eig2 + eig3) * 0.5;
     const double Mstar = (eig2 - eig3) * 0.5 * iam;
-    const double dun = nx * (R.u - L.u) + ny * (R.v - L.v);
+    const double dun = fma(nx, du, ny * dv);
     const double dp = R.p - L.p;
     const double ae = astar - eig1;
     const double dUroe = fma(Mstar, dun, ae * dp * irm * (iam * iam));
     const double dProe = fma(Mstar, dp, ae * rm * dun);
     const double dUr = dUroe * rm;
-    F.x -= 0.5 * fma(eig1, dW0, dUr);
-    F.y -= 0.5 * fma(eig1, dW1, fma(dUr, um, dProe * nx));
-    F.z -= 0.5 * fma(eig1, dW2, fma(dUr, vm, dProe * ny));
-    F.w -= 0.5 * fma(eig1, dW3, fma(dUr, Hm, dProe * un));
-    F.x *= area;
-    F.y *= area;
-    F.z *= area;
-    F.w *= area;
+    const double h = 0.5 * area;
+    F.x = h * (F.x - fma(eig1, dW0, dUr));
+    F.y = h * (F.y - fma(eig1, dW1, fma(dUr, um, dProe * nx)));
+    F.z = h * (F.z - fma(eig1, dW2, fma(dUr, vm, dProe * ny)));
+    F.w = h * (F.w - fma(eig1, dW3, fma(dUr, Hm, dProe * un)));
     return F;
 }
 
@@ -125,7 +164,7 @@ __device__ __forceinline__ d4 llf_flux(const d4 UL, const d4 UR, const Prim& L, 
     const double hr = g.gam_over_ga1 * R.p * R.ir + 0.5 * (R.u * R.u + R.v * R.v);
     const double aL = fabs(unL) + sqrt(g.gamma * L.p * L.ir);
     const double aR = fabs(unR) + sqrt(g.gamma * R.p * R.ir);
-    const double lm = (aL > aR) ? aL : aR;
+    const double lm = dmax(aL, aR);
     const double hlen = 0.5 * length;
     return mk4(hlen * (ruL + ruR - lm * (UR.x - UL.x)),
                         hlen * (fma(ruL, L.u, nx * L.p) + fma(ruR, R.u, nx * R.p) - lm * (UR.y - UL.y)),
@@ -184,7 +223,7 @@ __device__ __forceinline__ bool ghost_farfield(const Prim& e, const double* fs, 
 // the Prandtl number is the reference's constant 0.72.
 __device__ __forceinline__ void viscous_flux(d4& F, const d4 U, const d4 gx, const d4 gy,
                                              double nx, double ny, double area, const Gas& g) {
-    const double ir = 1.0 / U.x;
+    const double ir = rcp(U.x);
     const double u = U.y * ir, v = U.z * ir, E = U.w * ir;
     const double dudx = ir * (gx.y - u * gx.x);
     const double dvdx = ir * (gx.z - v * gx.x);
@@ -195,7 +234,7 @@ __device__ __forceinline__ void viscous_flux(d4& F, const d4 U, const d4 gx, con
     const double T = g.inv_Cv * (E - 0.5 * (u * u + v * v));
     const double dTdx = (dEdx - u * dudx - v * dvdx) * g.inv_Cv;
     const double dTdy = (dEdy - u * dudy - v * dvdy) * g.inv_Cv;
-    const double mu = g.C1 * (T * sqrt(T)) / (T + 110.4);
+    const double mu = g.C1 * (T * sqrt(T)) * rcp(T + 110.4);
     const double div = dudx + dvdy;
     const double NMD = -2.0 / 3.0;
     const double txx = mu * fma(NMD, div, 2.0 * dudx);

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(256) k_alpha(const d4* __restrict__ prim, Mesh
     const double* gm = &m.e_geom[(size_t)e * 8];
     const double nx = __ldg(&gm[0]), ny = __ldg(&gm[1]), len = __ldg(&gm[2]), sqrt_len = __ldg(&gm[3]);
     const double un = w.y * (nx * len) + w.z * (ny * len);
-    const double ir = 1.0 / w.x;
+    const double ir = rcp(w.x);
     alpha[e] = fabs(un) + sqrt(g.gamma * w.w * ir) * sqrt_len;
     if (NS) {
         const double T = w.w / g.R * ir;
@@ -67,19 +67,16 @@ __global__ void __launch_bounds__(256) k_dt_cell(MeshView m, const double* __res
             a += __ldg(&alpha[e]);
             if (NS) a += __ldg(&alpha_vis[e]) * ivol;
         }
-        double d = CFL * vol / a;
-        dtc = (dtc < d) ? dtc : d;
+        const double d = CFL * vol * rcp(a);
+        dtc = dmin(dtc, d);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        double x = __shfl_xor_sync(0xffffffffu, dtc, o);
-        dtc = (x < dtc) ? x : dtc;
-    }
+    for (int o = 16; o > 0; o >>= 1) dtc = dmin(dtc, __shfl_xor_sync(0xffffffffu, dtc, o));
     __shared__ double sm[8];
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = dtc;
     __syncthreads();
     if (threadIdx.x == 0) {
         double v = sm[0];
-        for (int i = 1; i < (int)(blockDim.x >> 5); i++) v = (sm[i] < v) ? sm[i] : v;
+        for (int i = 1; i < (int)(blockDim.x >> 5); i++) v = dmin(v, sm[i]);
         if (v >= 0) dmin_atomic(dtmin, v);
         else atomicMin(dtmin, 0ull);  // a negative time step cannot be represented; treat as 0
     }
@@ -118,6 +115,15 @@ __global__ void __launch_bounds__(256) k_grad(const d4* __restrict__ U, MeshView
     }
     double gx[4], gy[4];
     const double ucv[4] = {uc.x, uc.y, uc.z, uc.w};
+    // neighbour differences U_k - U_c (valid neighbours in slot order), shared by the
+    // least-squares gradient and the limiter's bounds
+    double dU[3][4];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const double unv[4] = {un[k].x, un[k].y, un[k].z, un[k].w};
+#pragma unroll
+        for (int v = 0; v < 4; v++) dU[k][v] = unv[v] - ucv[v];
+    }
     if (GRAD == 1) {
         // GradientLeastSquare_2 (Gradient.cpp:160-246) with the weights B = (A^T A)^-1 A^T
         // precomputed per cell: grad = B dU, summed over the valid neighbours in slot order
@@ -130,18 +136,9 @@ __global__ void __launch_bounds__(256) k_grad(const d4* __restrict__ U, MeshView
         }
 #pragma unroll
         for (int v = 0; v < 4; v++) {
-            double sx = 0.0, sy = 0.0;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                if (k < nnb) {
-                    const double unv = (v == 0) ? un[k].x : (v == 1) ? un[k].y : (v == 2) ? un[k].z : un[k].w;
-                    const double d = unv - ucv[v];
-                    sx = fma(b0[k], d, sx);
-                    sy = fma(b1[k], d, sy);
-                }
-            }
-            gx[v] = sx;
-            gy[v] = sy;
+            // absent neighbours carry B = 0 and dU = 0
+            gx[v] = fma(b0[2], dU[2][v], fma(b0[1], dU[1][v], b0[0] * dU[0][v]));
+            gy[v] = fma(b1[2], dU[2][v], fma(b1[1], dU[1][v], b1[0] * dU[0][v]));
         }
     } else {
         // GradientGreenGauss_2 (Gradient.cpp:248-458) with precomputed face weights
@@ -170,10 +167,15 @@ __global__ void __launch_bounds__(256) k_grad(const d4* __restrict__ U, MeshView
         }
     }
     if (BARTH) {
-        // LimiterBarth, Gradient.cpp:58-114.  The minimum over the vertices of
-        // min(1, dU+/(d+eps)) is taken at the largest positive vertex increment
-        // (and likewise for negative ones): division and rounding are monotonic,
-        // so one division per sign gives the same value as three.
+        // LimiterBarth, Gradient.cpp:58-114:
+        //   phi = min over the vertices of min(1, (hi - Uc)/(d + eps)) for d > 0 and
+        //   min(1, (lo - Uc)/(d - eps)) for d < 0, d = U(vertex) - Uc.
+        // hi - Uc and lo - Uc are the largest / smallest of 0 and the neighbour
+        // differences.  Division and rounding are monotonic, so the minimum over the
+        // positive vertices is taken at the largest d (and over the negative ones at
+        // the smallest d); of the two candidates only the smaller ratio is divided
+        // out (compared by cross-multiplication), and none when neither is below 1.
+        // All comparisons run on the integer pipe (okey).
         const double* X = &m.c_vtx[(size_t)c * 6];
         double vx[3], vy[3];
 #pragma unroll
@@ -183,47 +185,29 @@ __global__ void __launch_bounds__(256) k_grad(const d4* __restrict__ U, MeshView
         }
 #pragma unroll
         for (int v = 0; v < 4; v++) {
-            double lo = ucv[v], hi = ucv[v];
+            double np = 0.0, nn = 0.0;  // hi - Uc >= 0, lo - Uc <= 0
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 if (k < nnb) {
-                    const double unv = (v == 0) ? un[k].x : (v == 1) ? un[k].y : (v == 2) ? un[k].z : un[k].w;
-                    lo = (lo < unv) ? lo : unv;
-                    hi = (hi > unv) ? hi : unv;
+                    np = dmax(np, dU[k][v]);
+                    nn = dmin(nn, dU[k][v]);
                 }
             }
-            double dpos = 0.0, dneg = 0.0;
-            bool has_pos = false, has_neg = false;
-#pragma unroll
-            for (int j = 0; j < 3; j++) {
-                const double Un = fma(gy[v], vy[j], fma(gx[v], vx[j], ucv[v]));
-                const double dn = Un - ucv[v];
-                if (dn > 0) {
-                    dpos = has_pos ? ((dn > dpos) ? dn : dpos) : dn;
-                    has_pos = true;
-                } else if (dn < 0) {
-                    dneg = has_neg ? ((dn < dneg) ? dn : dneg) : dn;
-                    has_neg = true;
-                }
+            const double d0 = fma(gx[v], vx[0], gy[v] * vy[0]);
+            const double d1 = fma(gx[v], vx[1], gy[v] * vy[1]);
+            const double d2 = fma(gx[v], vx[2], gy[v] * vy[2]);
+            const double dhi = dmax(dmax(d0, d1), d2), dlo = dmin(dmin(d0, d1), d2);
+            const double dp = dhi + kEps, dn = dlo - kEps;
+            const bool lim_p = pos(dhi) && dlt(np, dp);  // ratio np/dp below 1
+            const bool lim_n = neg(dlo) && dlt(dn, nn);  // ratio nn/dn below 1
+            if (lim_p || lim_n) {
+                // both limited: np/dp < nn/dn  <=>  np*dn > nn*dp  (dp > 0 > dn)
+                const bool use_p = lim_p && (!lim_n || dlt(nn * dp, np * dn));
+                const double num = use_p ? np : nn, den = use_p ? dp : dn;
+                const double phi = num * rcp(den);
+                gx[v] *= phi;
+                gy[v] *= phi;
             }
-            double phi = 1.0;
-            if (has_pos) {
-                const double den = dpos + kEps, num = hi - ucv[v];
-                if (!(num >= den)) {
-                    const double r = num / den;
-                    phi = (r < 1.0) ? r : 1.0;
-                }
-            }
-            if (has_neg) {
-                const double den = dneg - kEps, num = lo - ucv[v];
-                if (!(num <= den)) {
-                    const double r = num / den;
-                    const double q = (r < 1.0) ? r : 1.0;
-                    phi = (phi < q) ? phi : q;
-                }
-            }
-            gx[v] *= phi;
-            gy[v] *= phi;
         }
     }
     Gx[c] = mk4(gx[0], gx[1], gx[2], gx[3]);
@@ -409,7 +393,7 @@ __global__ void __launch_bounds__(256) k_update(d4* __restrict__ U, const d4* __
         rhs_out[c] = k;
         // detection half of modifyElementFieldU2d (FVMR/src/space/restrict/Restrict.cpp:20-38)
         const Prim w = to_prim(un, g);
-        if (isnan(w.r) || isnan(w.u) || isnan(w.v) || isnan(w.p)) {
+        if (is_nan(w.r) || is_nan(w.u) || is_nan(w.v) || is_nan(w.p)) {
             atomicAdd(&st->nan_cells, 1ull);
         } else if (out_of_range(w.r, w.p)) {
             unsigned int slot = atomicAdd(flag_count, 1u);
