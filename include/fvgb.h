@@ -158,6 +158,24 @@ int fvgb_step_timed(fvgb_handle* h, double T, int nsteps, double* ms_out);
  * std::chrono, FVMR/src/drivers/CDriver.cpp:73-85.) */
 int fvgb_profile_steps(fvgb_handle* h, double T, int nsteps, double ms_out[5], int count_out[5]);
 
+/* No counterpart in the reference.  The first-order residual (constant
+ * reconstruction, Euler equations, Roe or LLF, every boundary type of this
+ * path) computed from device arrays the caller owns, without allocating any
+ * device or pinned memory: for callers that already manage every GPU buffer
+ * themselves and may not add allocations of their own.  dev_mesh holds DEVICE
+ * pointers to the reference-layout arrays (elem_edges, elem_volume, edge_L,
+ * edge_R, edge_setID, edge_length, edge_normal, boundary_type are read);
+ * U_dev is U[4][N] and rhs_dev receives RHS[4][N] = -(1/vol) sum of edge
+ * fluxes, both on the device; stream is a cudaStream_t (NULL = default
+ * stream); the call only enqueues work.  The edge fluxes are kept in one
+ * library-wide device array of 32 MiB (at most 1,048,576 edges; larger meshes
+ * get FVGB_ERR_ARG).  Every call shares that array, so calls that may overlap
+ * on the GPU must be serialised by the caller.  The first call on each device
+ * looks up the array's device address (a CUDA runtime query, no allocation).
+ * Far-field ghost states out of range are not reported by this call. */
+int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params* p, const double* U_dev, double* rhs_dev,
+                     void* stream);
+
 const char* fvgb_last_error(void);
 const char* fvgb_version(void);
 
