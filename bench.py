@@ -46,7 +46,63 @@ def parse():
     ap.add_argument("--n", type=int, default=N_SIDE, help="cells per side of the square (default 1448)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", choices=["vortex_large", "batch"], default="vortex_large",
+                    help="batch: many cylinder instances in one persistent launch per stage vs the same "
+                         "instances stepped one after another through the plain path")
+    ap.add_argument("--batch-n", type=int, default=256)
     return ap.parse_args()
+
+
+def run_batch(args):
+    """Batched cylinder instances (cells log-uniform in [5k, 200k], Mach in [0.1, 0.6], Euler, Roe,
+    LSQ + Barth, Kutta RK3): one persistent launch per stage in a graph, against the same instances
+    stepped one after another through the plain path."""
+    import torch
+    torch.cuda.set_device(0)
+    import cfd_solver_2d_gpu_gb300 as fv
+    from cfd_solver_2d_gpu_gb300 import cases
+    with tempfile.TemporaryDirectory() as d:
+        insts = cases.cylinder_batch(d, n=args.batch_n)
+        meshes, params = [], []
+        for tp, sp, _ in insts:
+            p = fv.Params.from_toml(tp)
+            meshes.append(fv.Mesh.read_su2(sp, p))
+            params.append(p)
+    cells = sum(m.N for m in meshes)
+    b = fv.Batch(meshes, params)
+    report = b.tune(2)
+    b.step_timed(args.warmup)
+    with ClockSampler(0) as clk:
+        ms_batch = b.step_timed(args.steps)
+    info = b.info()
+    clocks = clk.summary()
+    # the same instances, one after another through the plain path
+    ms_seq = 0.0
+    launches_seq = 0
+    for m, p in zip(meshes, params):
+        s = fv.GPUSolver2(m, p)
+        s.step_timed(p.T_end, 1)
+        l0 = s.kernel_launches()
+        ms_seq += s.step_timed(p.T_end, args.steps)
+        launches_seq += s.kernel_launches() - l0
+        s.close()
+    value = 3.0 * cells * args.steps / (ms_batch / 1e3)
+    seq = 3.0 * cells * args.steps / (ms_seq / 1e3)
+    line = {"metric": JSON_METRIC + " [batched form]", "value": value, "unit": "cell-stage updates/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batch / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (generated O-grids)",
+            "config": {"workload": f"{len(meshes)} cylinder O-grid instances, {cells} cells in total "
+                                   f"(log-uniform 5k-200k each, n_theta = 2 n_r), Mach U[0.1, 0.6], Euler, Roe, "
+                                   f"LSQ + Barth, Kutta RK3, CFL 0.5"},
+            "clocks": clocks, "gpu_launches": 3 * args.steps,
+            "batch": {"persistent_launches_per_step": 3, "graph": bool(info["graph"]), "grid": info["grid"],
+                      "block": info["block"], "tile": abs(info["tile"]),
+                      "schedule": "queue" if info["tile"] < 0 else "static", "autotuner": report.strip().split("\n")},
+            "sequential_plain": {"value": seq, "ms_per_step": ms_seq / args.steps,
+                                 "kernel_launches_per_step": launches_seq / args.steps},
+            "speedup_vs_sequential": ms_seq / ms_batch}
+    print(json.dumps(line), flush=True)
 
 
 def dist_env():
@@ -212,6 +268,10 @@ def run_reference(args, rank, world):
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "batch" and args.impl == "ours":
+        if rank == 0:
+            run_batch(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return

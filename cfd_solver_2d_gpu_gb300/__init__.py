@@ -109,6 +109,14 @@ def lib():
             "fvgb_kernel_launches": (ctypes.c_longlong, [v]),
             "fvgb_profile_steps": (i, [v, d, i, dp, ip]),
             "fvgb_step_timed": (i, [v, d, i, dp]),
+            "fvgb_batch_create": (i, [i, ctypes.POINTER(ctypes.POINTER(MeshSoA)), v, ctypes.POINTER(v)]),
+            "fvgb_batch_destroy": (None, [v]),
+            "fvgb_batch_set_state": (i, [v, i, dp]),
+            "fvgb_batch_get_state": (i, [v, i, dp]),
+            "fvgb_batch_step": (i, [v, dp, dp, i]),
+            "fvgb_batch_step_timed": (i, [v, i, dp]),
+            "fvgb_batch_tune": (i, [v, i, c, i]),
+            "fvgb_batch_info": (i, [v, ctypes.POINTER(ctypes.c_longlong)]),
             "fvgb_last_error": (c, []),
             "fvgb_version": (c, []),
         }
@@ -310,3 +318,58 @@ class GPUSolver2:
         cnt = np.zeros(5, dtype=np.int32)
         _check(lib().fvgb_profile_steps(self._h, float(T), int(nsteps), _dp(ms), _ip(cnt)))
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.PROFILE_GROUPS)}
+
+
+class Batch:
+    """Many Euler instances (fvgb_batch): one persistent launch per Runge-Kutta stage."""
+
+    def __init__(self, meshes, params_list):
+        if len(meshes) != len(params_list) or not meshes:
+            raise ValueError("one parameter set per mesh")
+        self.meshes, self.params = list(meshes), list(params_list)
+        self.n = len(meshes)
+        arr_m = (ctypes.POINTER(MeshSoA) * self.n)(*[ctypes.pointer(m.soa) for m in self.meshes])
+        arr_p = (Params * self.n)(*self.params)
+        self._h = ctypes.c_void_p()
+        _check(lib().fvgb_batch_create(self.n, arr_m, ctypes.cast(arr_p, ctypes.c_void_p), ctypes.byref(self._h)))
+        self.t = np.zeros(self.n)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fvgb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, i, U):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        _check(lib().fvgb_batch_set_state(self._h, int(i), _dp(U)))
+
+    def get_state(self, i):
+        U = np.empty((4, self.meshes[i].N))
+        _check(lib().fvgb_batch_get_state(self._h, int(i), _dp(U)))
+        return U
+
+    def step(self, nsteps, T=None):
+        t = np.ascontiguousarray(self.t, dtype=np.float64)
+        TT = None if T is None else np.ascontiguousarray(T, dtype=np.float64)
+        _check(lib().fvgb_batch_step(self._h, _dp(t), _dp(TT), int(nsteps)))
+        self.t = t
+        return t
+
+    def step_timed(self, nsteps):
+        ms = ctypes.c_double()
+        _check(lib().fvgb_batch_step_timed(self._h, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    def tune(self, trial_steps=2):
+        buf = ctypes.create_string_buffer(8192)
+        _check(lib().fvgb_batch_tune(self._h, int(trial_steps), buf, 8192))
+        return buf.value.decode()
+
+    def info(self):
+        out = (ctypes.c_longlong * 8)()
+        _check(lib().fvgb_batch_info(self._h, out))
+        keys = ("instances", "cells", "edges", "grid", "block", "launches", "tile", "graph")
+        return dict(zip(keys, list(out)))

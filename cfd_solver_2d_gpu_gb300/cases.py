@@ -59,14 +59,14 @@ def toml_text(*, equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1,
     return "\n".join(lines)
 
 
-def cache_dir():
-    d = os.environ.get("FVGB_CACHE", os.path.join(tempfile.gettempdir(), "fvgb_meshes"))
+def cache_dir(directory=None):
+    d = directory or os.environ.get("FVGB_CACHE", os.path.join(tempfile.gettempdir(), "fvgb_meshes"))
     os.makedirs(d, exist_ok=True)
     return d
 
 
 def square_mesh(n, jitter=0.0, L=10.0, seed=JITTER_SEED, directory=None):
-    path = os.path.join(directory or cache_dir(), f"square_{n}_{jitter:g}_{seed}.su2")
+    path = os.path.join(cache_dir(directory), f"square_{n}_{jitter:g}_{seed}.su2")
     if not os.path.exists(path):
         tmp = path + f".{os.getpid()}.tmp"
         write_periodic_square(tmp, n, L, jitter, seed)
@@ -75,7 +75,7 @@ def square_mesh(n, jitter=0.0, L=10.0, seed=JITTER_SEED, directory=None):
 
 
 def cylinder_mesh(n_theta, n_r, r0=0.5, r1=20.0, first_dr=1e-3, directory=None):
-    path = os.path.join(directory or cache_dir(), f"cyl_{n_theta}_{n_r}_{r0:g}_{r1:g}_{first_dr:g}.su2")
+    path = os.path.join(cache_dir(directory), f"cyl_{n_theta}_{n_r}_{r0:g}_{r1:g}_{first_dr:g}.su2")
     if not os.path.exists(path):
         tmp = path + f".{os.getpid()}.tmp"
         write_cylinder(tmp, n_theta, n_r, r0, r1, first_dr)
@@ -111,3 +111,24 @@ def cylinder_ns(directory, n_theta=512, n_r=256, **kw):
                 ic_type=1, inf_mode=0, Ma=0.2, AoA=0.0, Re=100.0, Pr=0.72, ref_area=1.0)
     args.update(kw)
     return write_case(directory, f"cylinder_ns_{n_theta}_{n_r}", toml_text(**args), cylinder_mesh(n_theta, n_r))
+
+
+def cylinder_batch(directory, n=256, n_min=5000, n_max=200000, seed=20261203, first_dr=1e-3, **kw):
+    """Batched cylinder instances: cell counts log-uniform in [n_min, n_max]
+    (n_r = round(sqrt(N/4)), n_theta = 2 n_r), freestream Mach uniform in
+    [0.1, 0.6]; inviscid (the wall is a slip wall), Roe, LSQ + Barth, RK3.
+    Returns a list of (toml path, su2 path, Mach)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n))
+    machs = rng.uniform(0.1, 0.6, n)
+    out = []
+    for i, (sz, ma) in enumerate(zip(sizes, machs)):
+        nr = max(2, int(round(np.sqrt(sz / 4.0))))
+        args = dict(equation=1, flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3103, CFL=0.5,
+                    ic_type=1, inf_mode=0, Ma=float(ma), AoA=0.0, T_end=1e9)
+        args.update(kw)
+        tp, sp = write_case(directory, f"batch_{i}", toml_text(**args),
+                            cylinder_mesh(2 * nr, nr, first_dr=first_dr, directory=directory))
+        out.append((tp, sp, float(ma)))
+    return out

@@ -3,20 +3,10 @@
 #include <cuda_runtime.h>
 
 #include "kernels.cuh"
+#include "step_device.cuh"
 
 namespace fvgb {
 namespace dev {
-
-enum StageKind {
-    STAGE_RHS = 0,     // residual only
-    STAGE_EULER = 1,   // forward Euler (3101)
-    STAGE_RK3_1 = 2,   // Kutta RK3 (3103) stages
-    STAGE_RK3_2 = 3,
-    STAGE_RK3_3 = 4,
-    STAGE_SSP_1 = 5,   // SSP-RK3 (3104) stages
-    STAGE_SSP_2 = 6,
-    STAGE_SSP_3 = 7,
-};
 
 // Time and time step of one solver, kept on the device so a step needs no host sync.
 struct StepState {

@@ -158,6 +158,32 @@ int fvgb_step_timed(fvgb_handle* h, double T, int nsteps, double* ms_out);
  * std::chrono, FVMR/src/drivers/CDriver.cpp:73-85.) */
 int fvgb_profile_steps(fvgb_handle* h, double T, int nsteps, double ms_out[5], int count_out[5]);
 
+/* ---- batched instances -----------------------------------------------------
+ * No counterpart in the reference (one mesh per process, the driver loop of
+ * FVMR/src/drivers/CDriver.cpp:75-80 stepping it).  n independent instances of
+ * the Euler step (their own meshes, far-field states, CFL, time and end time;
+ * one shared scheme) packed into one device layout and advanced by one
+ * persistent cooperative kernel per Runge-Kutta stage, the step captured in a
+ * CUDA graph.  Each instance gives bit for bit what fvgb_step gives for it
+ * alone.  States are in each instance's reference numbering. */
+int fvgb_batch_create(int n, const fvgb_mesh_soa* const* meshes, const fvgb_params* params, fvgb_batch** out);
+void fvgb_batch_destroy(fvgb_batch* b);
+int fvgb_batch_set_state(fvgb_batch* b, int i, const double* U);
+int fvgb_batch_get_state(fvgb_batch* b, int i, double* U);
+/* nsteps steps of every instance; t[n] is read and updated, T[n] (may be NULL
+ * to keep the end times of the parameters) clamps each instance's time. */
+int fvgb_batch_step(fvgb_batch* b, double* t, const double* T, int nsteps);
+/* nsteps with the times kept on the device, bracketed by CUDA events. */
+int fvgb_batch_step_timed(fvgb_batch* b, int nsteps, double* ms_out);
+/* The autotuner: times block size x work-tile size x static or queued tile
+ * schedule on trial_steps steps of this batch (state restored afterwards) and
+ * keeps the fastest; report gets one line per candidate. */
+int fvgb_batch_tune(fvgb_batch* b, int trial_steps, char* report, int report_len);
+/* [0] instances, [1] cells, [2] edges, [3] grid, [4] block, [5] kernel
+ * launches, [6] tile size (negative: queued schedule), [7] 1 if the step runs
+ * as a captured graph. */
+int fvgb_batch_info(fvgb_batch* b, long long out[8]);
+
 /* No counterpart in the reference.  The first-order residual (constant
  * reconstruction, Euler equations, Roe or LLF, every boundary type of this
  * path) computed from device arrays the caller owns, without allocating any

@@ -1,0 +1,81 @@
+"""The batched form (fvgb_batch_*): instances of uneven size packed into one
+persistent launch per Runge-Kutta stage give, bit for bit, what each instance
+gives when stepped alone through the plain path; the autotuner leaves the state
+untouched."""
+import numpy as np
+import pytest
+
+import cfd_solver_2d_gpu_gb300 as fv
+from cfd_solver_2d_gpu_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def load(tp, sp):
+    p = fv.Params.from_toml(tp)
+    return fv.Mesh.read_su2(sp, p), p
+
+
+def cylinders(tmp_path, nrs, machs, **kw):
+    out = []
+    for i, (nr, ma) in enumerate(zip(nrs, machs)):
+        args = dict(equation=1, flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3103, CFL=0.5,
+                    ic_type=1, inf_mode=0, Ma=ma, AoA=0.0, T_end=1e9)
+        args.update(kw)
+        tp, sp = cases.write_case(str(tmp_path), f"c{i}", cases.toml_text(**args),
+                                  cases.cylinder_mesh(2 * nr, nr, directory=str(tmp_path)))
+        out.append(load(tp, sp))
+    return out
+
+
+def plain_run(mesh, p, steps):
+    s = fv.GPUSolver2(mesh, p)
+    t = s.step(0.0, p.T_end, steps)
+    return s.get_state(), t
+
+
+def test_batch_matches_plain_cylinders(tmp_path):
+    inst = cylinders(tmp_path, [6, 9, 12, 7, 10], [0.15, 0.3, 0.45, 0.55, 0.2])
+    b = fv.Batch([m for m, _ in inst], [p for _, p in inst])
+    t = b.step(4)
+    info = b.info()
+    assert info["instances"] == 5 and info["launches"] == 12
+    for i, (m, p) in enumerate(inst):
+        U, tp = plain_run(m, p, 4)
+        assert np.array_equal(b.get_state(i), U), i
+        assert t[i] == tp
+
+
+def test_batch_matches_plain_vortex_ssp_gg_llf(tmp_path):
+    inst = []
+    for n in (8, 16, 12):
+        tp, sp = cases.write_case(str(tmp_path), f"v{n}", cases.toml_text(
+            flux=2001, reconstruct=3002, gradient=2, limiter=1, time_advance=3104, CFL=0.8),
+            cases.square_mesh(n, jitter=0.2, directory=str(tmp_path)))
+        inst.append(load(tp, sp))
+    b = fv.Batch([m for m, _ in inst], [p for _, p in inst])
+    b.step(3)
+    for i, (m, p) in enumerate(inst):
+        U, _ = plain_run(m, p, 3)
+        assert np.array_equal(b.get_state(i), U), i
+
+
+def test_autotuner_keeps_state_and_result(tmp_path):
+    inst = cylinders(tmp_path, [8, 14, 5], [0.1, 0.4, 0.6])
+    b = fv.Batch([m for m, _ in inst], [p for _, p in inst])
+    before = [b.get_state(i) for i in range(3)]
+    report = b.tune(1)
+    assert report.count("ms/step") >= 4 and "chosen" in report
+    for i in range(3):
+        assert np.array_equal(b.get_state(i), before[i])
+    b.step(2)
+    for i, (m, p) in enumerate(inst):
+        U, _ = plain_run(m, p, 2)
+        assert np.array_equal(b.get_state(i), U), i
+
+
+def test_batch_rejects_mixed_schemes(tmp_path):
+    a = cylinders(tmp_path, [5], [0.2])[0]
+    c = cylinders(tmp_path, [5], [0.2], flux=2001)[0]
+    with pytest.raises(fv.FvgbError):
+        fv.Batch([a[0], c[0]], [a[1], c[1]])
