@@ -46,11 +46,106 @@ def parse():
     ap.add_argument("--n", type=int, default=N_SIDE, help="cells per side of the square (default 1448)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=["vortex_large", "batch"], default="vortex_large",
+    ap.add_argument("--workload", choices=["vortex_large", "batch", "adjoint"], default="vortex_large",
                     help="batch: many cylinder instances in one persistent launch per stage vs the same "
-                         "instances stepped one after another through the plain path")
+                         "instances stepped one after another through the plain path; adjoint: the discrete "
+                         "adjoint through K SSP-RK3 steps on the 256x256 jittered vortex")
     ap.add_argument("--batch-n", type=int, default=256)
+    ap.add_argument("--adjoint-k", type=int, default=500)
+    ap.add_argument("--fd-directions", type=int, default=64)
+    ap.add_argument("--oracle-directions", type=int, default=0)
     return ap.parse_args()
+
+
+def run_adjoint(args):
+    """Discrete adjoint through K SSP-RK3 steps (256x256 jittered vortex, 131,072 cells, LSQ + Barth,
+    Roe): time ratio to the primal, and central finite differences (step 1e-6) on random directions."""
+    import torch
+    torch.cuda.set_device(0)
+    import cfd_solver_2d_gpu_gb300 as fv
+    from cfd_solver_2d_gpu_gb300 import adjoint_backward, adjoint_forward, cases
+    K = args.adjoint_k
+    with tempfile.TemporaryDirectory() as d:
+        su2 = cases.square_mesh(256, jitter=0.2, directory=d)
+        tp = os.path.join(d, "adj.toml")
+        with open(tp, "w") as f:
+            f.write(cases.toml_text(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.8))
+        p = fv.Params.from_toml(tp)
+        mesh = fv.Mesh.read_su2(su2, p)
+        s = fv.GPUSolver2(mesh, p)
+        U0 = s.get_state()
+        rng = np.random.default_rng(20261203)
+        r = rng.uniform(-1, 1, 3)
+        pt = fv.Params.from_toml(tp)
+        pt.vortex[0], pt.vortex[1], pt.vortex[2] = 5 + 0.1 * r[1], 5 + 0.1 * r[2], 5 * (1 + 0.02 * r[0])
+        Ut0 = fv.initial_field(mesh, pt)
+
+        def fwd(U):
+            s.set_state(U)
+            s.set_time(0.0)
+            s.step_timed(p.T_end, K)
+            return s.get_state()
+
+        rho_t = fwd(Ut0)[0]
+        s.set_state(U0)
+        s.set_time(0.0)
+        s.step_timed(p.T_end, 3)  # warm-up
+        s.set_state(U0)
+        s.set_time(0.0)
+        ms_primal = s.step_timed(p.T_end, K)
+        nck = max(1, int(round(np.sqrt(K))))
+        adjoint_forward(s, U0, K, nck)  # warm-up of the adjoint path
+        t0 = time.perf_counter()
+        UK, ms_f = adjoint_forward(s, U0, K, nck)
+        dd = UK[0] - rho_t
+        seed = np.zeros_like(UK)
+        seed[0] = dd
+        g, ms_b = adjoint_backward(s, seed)
+        wall = time.perf_counter() - t0
+        L0 = 0.5 * float(dd @ dd)
+
+        def loss(U):
+            x = fwd(U)[0] - rho_t
+            return 0.5 * float(x @ x)
+
+        h = 1e-6
+        errs = []
+        drng = np.random.default_rng(64)
+        dirs = []
+        for _ in range(args.fd_directions):
+            v = drng.standard_normal(U0.shape)
+            v /= np.linalg.norm(v)
+            dirs.append(v)
+            fd = (loss(U0 + h * v) - loss(U0 - h * v)) / (2 * h)
+            errs.append(abs(fd - float(np.sum(g * v))) / max(abs(fd), 1e-300))
+        ref_errs = []
+        if args.oracle_directions > 0:
+            from oracle import pyoracle
+            pyoracle.set_threads(os.cpu_count() or 1)
+            o = pyoracle.Oracle(tp, su2)
+            rho_to = o.run(Ut0, K)[0][0]
+
+            def oloss(U):
+                x = o.run(U, K)[0][0] - rho_to
+                return 0.5 * float(x @ x)
+            for v in dirs[: args.oracle_directions]:
+                fd = (oloss(U0 + h * v) - oloss(U0 - h * v)) / (2 * h)
+                ref_errs.append(abs(fd - float(np.sum(g * v))) / max(abs(fd), 1e-300))
+    errs = np.array(errs)
+    line = {"metric": "adjoint-to-primal time ratio (1 GB300, FP64)", "value": (ms_f + ms_b) / ms_primal,
+            "unit": "x", "higher_is_better": False, "n_gpus": 1, "steps": K, "dtype": "f64",
+            "data": "synthetic (generated mesh and initial field of the configuration's shape)",
+            "config": {"workload": f"discrete adjoint through {K} SSP-RK3 steps, 256x256 jittered vortex "
+                                   f"({mesh.N} cells), LSQ + Barth, Roe, CFL 0.8, {nck} checkpoints",
+                       "loss": "1/2 ||rho_K - rho_target||^2, target from a perturbed vortex"},
+            "primal_ms": ms_primal, "adjoint_forward_ms": ms_f, "adjoint_backward_ms": ms_b,
+            "ratio_backward_to_primal": ms_b / ms_primal, "wall_s": wall, "loss": L0,
+            "fd": {"step": h, "directions": len(errs), "median_rel_err": float(np.median(errs)),
+                   "max_rel_err": float(errs.max()), "frac_below_1e-6": float(np.mean(errs < 1e-6))},
+            "reference_gradient": {"directions": len(ref_errs),
+                                   "max_rel_err": float(max(ref_errs)) if ref_errs else None,
+                                   "source": "central differences of the oracle's forward map"}}
+    print(json.dumps(line), flush=True)
 
 
 def run_batch(args):
@@ -271,6 +366,10 @@ def main():
     if args.workload == "batch" and args.impl == "ours":
         if rank == 0:
             run_batch(args)
+        return
+    if args.workload == "adjoint" and args.impl == "ours":
+        if rank == 0:
+            run_adjoint(args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -373,3 +373,36 @@ class Batch:
         _check(lib().fvgb_batch_info(self._h, out))
         keys = ("instances", "cells", "edges", "grid", "block", "launches", "tile", "graph")
         return dict(zip(keys, list(out)))
+
+
+def _bind_adjoint():
+    L = lib()
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.fvgb_adjoint_forward.restype = ctypes.c_int
+    L.fvgb_adjoint_forward.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp, ctypes.c_double, dp, dp]
+    L.fvgb_adjoint_backward.restype = ctypes.c_int
+    L.fvgb_adjoint_backward.argtypes = [ctypes.c_void_p, dp, dp, dp]
+    L.fvgb_adjoint_release.restype = None
+    L.fvgb_adjoint_release.argtypes = [ctypes.c_void_p]
+    return L
+
+
+def adjoint_forward(solver, U0, nsteps, n_checkpoints=None, t0=0.0):
+    """K steps from U0 keeping checkpoints; returns (U_K, forward milliseconds)."""
+    L = _bind_adjoint()
+    U0 = np.ascontiguousarray(U0, dtype=np.float64)
+    UK = np.empty_like(U0)
+    ms = ctypes.c_double()
+    nck = n_checkpoints if n_checkpoints is not None else max(1, int(round(np.sqrt(nsteps))))
+    _check(L.fvgb_adjoint_forward(solver._h, int(nsteps), int(nck), _dp(U0), float(t0), _dp(UK), ctypes.byref(ms)))
+    return UK, ms.value
+
+
+def adjoint_backward(solver, seed):
+    """dL/dU_0 for the seed dL/dU_K of the last adjoint_forward; returns (grad, backward milliseconds)."""
+    L = _bind_adjoint()
+    seed = np.ascontiguousarray(seed, dtype=np.float64)
+    g = np.empty_like(seed)
+    ms = ctypes.c_double()
+    _check(L.fvgb_adjoint_backward(solver._h, _dp(seed), _dp(g), ctypes.byref(ms)))
+    return g, ms.value

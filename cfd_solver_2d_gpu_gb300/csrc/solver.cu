@@ -416,10 +416,6 @@ int Solver::residual(int norm, double* out) {
 
 using namespace fvgb;
 
-struct fvgb_handle {
-    Solver s;
-};
-
 #define GUARD(h)                                                     \
     do {                                                             \
         if (!(h)) return fail(FVGB_ERR_ARG, "null handle");          \
@@ -443,6 +439,7 @@ extern "C" int fvgb_create(const fvgb_mesh_soa* mesh, const fvgb_params* p, fvgb
 extern "C" void fvgb_destroy(fvgb_handle* h) {
     if (!h) return;
     cudaSetDevice(h->s.p.device);
+    fvgb_adjoint_release(h);  // the adjoint workspace of this handle, if any
     delete h;
 }
 

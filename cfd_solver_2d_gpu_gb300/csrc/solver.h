@@ -76,3 +76,9 @@ struct Solver {
 };
 
 }  // namespace fvgb
+
+// the C ABI's opaque handle: one solver
+struct fvgb_handle {
+    fvgb::Solver s;
+};
+

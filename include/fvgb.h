@@ -158,6 +158,22 @@ int fvgb_step_timed(fvgb_handle* h, double T, int nsteps, double* ms_out);
  * std::chrono, FVMR/src/drivers/CDriver.cpp:73-85.) */
 int fvgb_profile_steps(fvgb_handle* h, double T, int nsteps, double ms_out[5], int count_out[5]);
 
+/* ---- discrete adjoint ------------------------------------------------------
+ * No counterpart in the reference.  Reverse-mode derivative of K steps of the
+ * handle's own step map U_0 -> U_K (Euler equations, Roe flux, least-squares
+ * gradients with or without the Barth limiter, forward Euler or SSP-RK3,
+ * interior / periodic / slip-wall edges; the time step's dependence on the
+ * state included).  fvgb_adjoint_forward runs the K steps from U0 at time t0
+ * keeping n_checkpoints states (sqrt(K) keeps memory at O(sqrt(K) N)) and
+ * returns U_K; fvgb_adjoint_backward then maps a seed dL/dU_K to dL/dU_0
+ * (both [4][N], reference numbering), recomputing each segment once.  The
+ * handle's state afterwards is U_K.  Fails with FVGB_ERR_UNSUPPORTED outside
+ * that scope, and when the positivity pass acted during the run. */
+int fvgb_adjoint_forward(fvgb_handle* h, int nsteps, int n_checkpoints, const double* U0, double t0, double* U_K,
+                         double* ms_forward);
+int fvgb_adjoint_backward(fvgb_handle* h, const double* seed_UK, double* grad_U0, double* ms_backward);
+void fvgb_adjoint_release(fvgb_handle* h);
+
 /* ---- batched instances -----------------------------------------------------
  * No counterpart in the reference (one mesh per process, the driver loop of
  * FVMR/src/drivers/CDriver.cpp:75-80 stepping it).  n independent instances of

@@ -1,0 +1,144 @@
+"""The discrete adjoint (fvgb_adjoint_forward / fvgb_adjoint_backward) against
+central finite differences of the same forward map (step 1e-6, random unit
+directions), against finite differences of the oracle's forward map (the
+reference gradient), under different checkpoint counts, and through the
+torch.autograd.Function wrapper.
+
+Loss: L = 1/2 sum_c (rho_K(c) - rho_target(c))^2, the target being the
+forward solution from a perturbed initial state (vortex strength and centre
+shifted by seeded amounts)."""
+import numpy as np
+import pytest
+
+import cfd_solver_2d_gpu_gb300 as fv
+from cfd_solver_2d_gpu_gb300 import adjoint_backward, adjoint_forward, cases
+from oracle.pyoracle import Oracle
+
+pytestmark = pytest.mark.gpu
+H = 1e-6
+
+
+def setup_case(tmp_path, n=24, jitter=0.2, time_advance=3104, reconstruct=3002, limiter=1, walls=False, CFL=0.8):
+    su2 = cases.square_mesh(n, jitter=jitter, directory=str(tmp_path))
+    if walls:  # periodic left/right, slip walls top and bottom
+        text = open(su2).read().replace("MARKER_TAG= periodic_2", "MARKER_TAG= wall")
+        su2 = str(tmp_path / f"channel_{n}.su2")
+        open(su2, "w").write(text)
+    tp = str(tmp_path / f"adj_{n}_{time_advance}_{reconstruct}_{limiter}_{walls}.toml")
+    with open(tp, "w") as f:
+        f.write(cases.toml_text(flux=2002, reconstruct=reconstruct, gradient=1, limiter=limiter,
+                                time_advance=time_advance, CFL=CFL))
+    p = fv.Params.from_toml(tp)
+    mesh = fv.Mesh.read_su2(su2, p)
+    solver = fv.GPUSolver2(mesh, p)
+    U0 = solver.get_state()
+    # target: vortex strength 5 (1 + 0.02 r1), centre (5 + 0.1 r2, 5 + 0.1 r3)
+    rng = np.random.default_rng(7)
+    r = rng.uniform(-1, 1, 3)
+    pt = fv.Params.from_toml(tp)
+    pt.vortex[0], pt.vortex[1], pt.vortex[2] = 5 + 0.1 * r[1], 5 + 0.1 * r[2], 5 * (1 + 0.02 * r[0])
+    Ut0 = fv.initial_field(mesh, pt)
+    return tp, su2, p, mesh, solver, U0, Ut0
+
+
+def forward(solver, p, U0, K):
+    solver.set_state(U0)
+    solver.step(0.0, p.T_end, K)
+    return solver.get_state()
+
+
+def loss_seed(UK, rho_t):
+    d = UK[0] - rho_t
+    seed = np.zeros_like(UK)
+    seed[0] = d
+    return 0.5 * float(np.dot(d, d)), seed
+
+
+def fd_check(solver, p, U0, rho_t, K, ndir, seed_rng=11, nck=None):
+    UK, _ = adjoint_forward(solver, U0, K, nck)
+    L0, seed = loss_seed(UK, rho_t)
+    g, _ = adjoint_backward(solver, seed)
+    rng = np.random.default_rng(seed_rng)
+    errs = []
+    for _ in range(ndir):
+        d = rng.standard_normal(U0.shape)
+        d /= np.linalg.norm(d)
+        Lp, _ = loss_seed(forward(solver, p, U0 + H * d, K), rho_t)
+        Lm, _ = loss_seed(forward(solver, p, U0 - H * d, K), rho_t)
+        fd = (Lp - Lm) / (2 * H)
+        ad = float(np.sum(g * d))
+        errs.append(abs(fd - ad) / max(abs(fd), 1e-30))
+    return np.array(errs), g
+
+
+def test_adjoint_matches_fd_second_order_ssp(tmp_path):
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path)
+    K = 10
+    rho_t = forward(solver, p, Ut0, K)[0]
+    errs, _ = fd_check(solver, p, U0, rho_t, K, 8)
+    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+
+
+def test_adjoint_matches_fd_first_order_euler(tmp_path):
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=16, jitter=0.0, time_advance=3101, reconstruct=3001,
+                                                   CFL=0.5)
+    K = 8
+    rho_t = forward(solver, p, Ut0, K)[0]
+    errs, _ = fd_check(solver, p, U0, rho_t, K, 6)
+    assert errs.max() <= 1e-6, errs
+
+
+def test_adjoint_slip_walls(tmp_path):
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=16, walls=True, limiter=0, CFL=0.5)
+    K = 6
+    rho_t = forward(solver, p, Ut0, K)[0]
+    errs, _ = fd_check(solver, p, U0, rho_t, K, 6)
+    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+
+
+def test_checkpoints_do_not_change_the_gradient(tmp_path):
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=16)
+    K = 9
+    rho_t = forward(solver, p, Ut0, K)[0]
+    grads = []
+    for nck in (1, 3, 9):
+        UK, _ = adjoint_forward(solver, U0, K, nck)
+        _, seed = loss_seed(UK, rho_t)
+        g, _ = adjoint_backward(solver, seed)
+        grads.append(g)
+    assert np.array_equal(grads[0], grads[1]) and np.array_equal(grads[1], grads[2])
+
+
+def test_against_oracle_finite_differences(tmp_path):
+    """The reference gradient: central differences of the oracle's forward map (CPU)."""
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=12)
+    K = 5
+    o = Oracle(tp, su2)
+    rho_t = o.run(Ut0, K)[0][0]
+    UK, _ = adjoint_forward(solver, U0, K)
+    _, seed = loss_seed(UK, rho_t)
+    g, _ = adjoint_backward(solver, seed)
+    rng = np.random.default_rng(3)
+    for _ in range(4):
+        d = rng.standard_normal(U0.shape)
+        d /= np.linalg.norm(d)
+        Lp, _ = loss_seed(o.run(U0 + H * d, K)[0], rho_t)
+        Lm, _ = loss_seed(o.run(U0 - H * d, K)[0], rho_t)
+        fd = (Lp - Lm) / (2 * H)
+        assert abs(fd - np.sum(g * d)) <= 1e-5 * abs(fd)
+
+
+def test_torch_autograd_function(tmp_path):
+    torch = pytest.importorskip("torch")
+    from cfd_solver_2d_gpu_gb300.autograd import steps
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=12)
+    K = 4
+    rho_t = torch.from_numpy(forward(solver, p, Ut0, K)[0])
+    x = torch.from_numpy(U0.copy()).requires_grad_(True)
+    UK = steps(x, solver, K)
+    loss = 0.5 * ((UK[0] - rho_t) ** 2).sum()
+    loss.backward()
+    UK2, _ = adjoint_forward(solver, U0, K)
+    _, seed = loss_seed(UK2, rho_t.numpy())
+    g, _ = adjoint_backward(solver, seed)
+    assert np.allclose(x.grad.numpy(), g, rtol=0, atol=1e-14 * np.abs(g).max())
