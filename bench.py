@@ -58,8 +58,8 @@ def parse():
 
 
 def run_adjoint(args):
-    """Discrete adjoint through K SSP-RK3 steps (256x256 jittered vortex, 131,072 cells, LSQ + Barth,
-    Roe): time ratio to the primal, and central finite differences (step 1e-6) on random directions."""
+    """Discrete adjoint through K SSP-RK3 steps (256x256 jittered vortex with smooth waves on
+    every variable, 131,072 cells, LSQ + Barth, Roe): time ratio to the primal, and central finite differences (step 1e-6) on random directions."""
     import torch
     torch.cuda.set_device(0)
     import cfd_solver_2d_gpu_gb300 as fv
@@ -73,12 +73,12 @@ def run_adjoint(args):
         p = fv.Params.from_toml(tp)
         mesh = fv.Mesh.read_su2(su2, p)
         s = fv.GPUSolver2(mesh, p)
-        U0 = s.get_state()
+        U0 = cases.wavy(mesh, s.get_state())
         rng = np.random.default_rng(20261203)
         r = rng.uniform(-1, 1, 3)
         pt = fv.Params.from_toml(tp)
         pt.vortex[0], pt.vortex[1], pt.vortex[2] = 5 + 0.1 * r[1], 5 + 0.1 * r[2], 5 * (1 + 0.02 * r[0])
-        Ut0 = fv.initial_field(mesh, pt)
+        Ut0 = cases.wavy(mesh, fv.initial_field(mesh, pt))
 
         def fwd(U):
             s.set_state(U)
@@ -132,16 +132,25 @@ def run_adjoint(args):
                 fd = (oloss(U0 + h * v) - oloss(U0 - h * v)) / (2 * h)
                 ref_errs.append(abs(fd - float(np.sum(g * v))) / max(abs(fd), 1e-300))
     errs = np.array(errs)
-    line = {"metric": "adjoint-to-primal time ratio (1 GB300, FP64)", "value": (ms_f + ms_b) / ms_primal,
+    # the forward sweep is the primal run itself (it produces U_K, which the loss needs) plus the
+    # checkpoint copies; the adjoint's own cost is that overhead plus the reverse sweep (which
+    # includes the recomputation of every segment but the last)
+    line = {"metric": "adjoint-to-primal time ratio (1 GB300, FP64)",
+            "value": (ms_f - ms_primal + ms_b) / ms_primal,
+            "definition": "(forward sweep with checkpoints - plain primal + reverse sweep) / plain primal, "
+                          "K steps each",
+            "total_ratio": (ms_f + ms_b) / ms_primal,
             "unit": "x", "higher_is_better": False, "n_gpus": 1, "steps": K, "dtype": "f64",
             "data": "synthetic (generated mesh and initial field of the configuration's shape)",
-            "config": {"workload": f"discrete adjoint through {K} SSP-RK3 steps, 256x256 jittered vortex "
+            "config": {"workload": f"discrete adjoint through {K} SSP-RK3 steps, 256x256 jittered vortex + waves "
                                    f"({mesh.N} cells), LSQ + Barth, Roe, CFL 0.8, {nck} checkpoints",
                        "loss": "1/2 ||rho_K - rho_target||^2, target from a perturbed vortex"},
             "primal_ms": ms_primal, "adjoint_forward_ms": ms_f, "adjoint_backward_ms": ms_b,
             "ratio_backward_to_primal": ms_b / ms_primal, "wall_s": wall, "loss": L0,
-            "fd": {"step": h, "directions": len(errs), "median_rel_err": float(np.median(errs)),
-                   "max_rel_err": float(errs.max()), "frac_below_1e-6": float(np.mean(errs < 1e-6))},
+            "fd": {"step": h, "directions": len(errs),
+                   "median_rel_err": float(np.median(errs)) if len(errs) else None,
+                   "max_rel_err": float(errs.max()) if len(errs) else None,
+                   "frac_below_1e-6": float(np.mean(errs < 1e-6)) if len(errs) else None},
             "reference_gradient": {"directions": len(ref_errs),
                                    "max_rel_err": float(max(ref_errs)) if ref_errs else None,
                                    "source": "central differences of the oracle's forward map"}}

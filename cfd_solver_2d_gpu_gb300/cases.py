@@ -83,6 +83,24 @@ def cylinder_mesh(n_theta, n_r, r0=0.5, r1=20.0, first_dr=1e-3, directory=None):
     return path
 
 
+def wavy(mesh, U, L=10.0):
+    """U with smooth multiplicative waves of period L on all four variables.
+
+    Used where the initial field must be non-uniform in every cell: the
+    isentropic vortex is uniform to ~1e-11 away from its core, where the Barth
+    limiter and the time-step minimum switch branch under tiny perturbations."""
+    import numpy as np
+    x, y = mesh.array("elem_xy")
+    k = 2 * np.pi / L
+    f = 1 + 0.05 * np.sin(k * x + 0.3) * np.cos(k * y + 0.7) + 0.03 * np.sin(2 * k * (x + y))
+    U = np.array(U, dtype=np.float64, copy=True)
+    U[0] *= f
+    U[1] *= 1 + 0.04 * np.cos(k * y)
+    U[2] *= 1 - 0.04 * np.sin(k * x)
+    U[3] *= f
+    return U
+
+
 def write_case(directory, name, toml, mesh_path):
     os.makedirs(directory, exist_ok=True)
     tp = os.path.join(directory, name + ".toml")

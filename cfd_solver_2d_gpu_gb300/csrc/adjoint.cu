@@ -15,10 +15,12 @@
 // states (sqrt(K) checkpoints: O(sqrt(K) N)).
 //
 // Kernels of one stage VJP (all gathers, no atomics: deterministic):
-//   primal gradient + limiter of the stage input (k_grad)
-//   k_adj_edge     per edge: face states, flux, flux VJP, mu = seed-weighted flux adjoint, F.mu
+//   k_adj_edge     per edge: face states, mu = seed-weighted flux adjoint, flux VJP
 //   k_adj_cell     per cell: gather the face-state adjoints of its edges; limiter + LSQ VJP
-//   k_adj_combine  per cell: gather the neighbours' LSQ adjoints; the stage's RK combination
+//   k_adj_combine  per cell: gather the neighbours' LSQ adjoints; the stage's RK combination;
+//                  block partials of lam_s . R_s (the time step's adjoint)
+// and once a step k_adj_dt.  The recorded forward keeps, per stage, the input state, the
+// limited gradients and the residual R_s, so no stage recomputes them.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,14 +37,16 @@ namespace fvgb {
 namespace dev {
 
 // ---- per edge --------------------------------------------------------------
+// 128-thread blocks: ~156 registers a thread leave room for three blocks per SM
+constexpr int kEdgeThreads = 128;
+
 template <bool LINEAR>
-__global__ void __launch_bounds__(256) k_adj_edge(const d4* __restrict__ U, const d4* __restrict__ Gx,
+__global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(const d4* __restrict__ U, const d4* __restrict__ Gx,
                                                   const d4* __restrict__ Gy, MeshView m, Gas g,
                                                   const d4* __restrict__ lam, const int* __restrict__ e_rlist,
-                                                  d4* __restrict__ aL, d4* __restrict__ aR, int* __restrict__ aflag,
-                                                  double* __restrict__ dot_part) {
+                                                  d4* __restrict__ aL, d4* __restrict__ aR,
+                                                  int* __restrict__ aflag) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    double dot = 0.0;
     if (e < m.E) {
         const int L = __ldg(&m.e_L[e]), R = __ldg(&m.e_R[e]);
         const double* gm = &m.e_geom[(size_t)e * 8];
@@ -63,12 +67,8 @@ __global__ void __launch_bounds__(256) k_adj_edge(const d4* __restrict__ U, cons
             gyL = ld4(&Gy[L]);
         }
         Prim wL;
-        const d4 fL = face_state<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL);
-        int flag = 0;  // bit 0 / bit 1: the L / R face state is the linear reconstruction
-        if (LINEAR) {
-            const Prim t = to_prim(lin(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5])), g);
-            if (!out_of_range(t.r, t.p)) flag |= 1;
-        }
+        bool usedL, usedR = false;
+        const d4 fL = face_state_used<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL, usedL);
         d4 bfL = mk4(0, 0, 0, 0), bfR = mk4(0, 0, 0, 0);
         Prim bwL{}, bwR{};
         if (e < m.E_int) {
@@ -79,40 +79,23 @@ __global__ void __launch_bounds__(256) k_adj_edge(const d4* __restrict__ U, cons
                 gyR = ld4(&Gy[R]);
             }
             Prim wR;
-            const d4 fR = face_state<LINEAR>(uR, gxR, gyR, __ldg(&gm[6]), __ldg(&gm[7]), g, wR);
-            if (LINEAR) {
-                const Prim t = to_prim(lin(uR, gxR, gyR, __ldg(&gm[6]), __ldg(&gm[7])), g);
-                if (!out_of_range(t.r, t.p)) flag |= 2;
-            }
-            const d4 F = roe_flux(wL, wR, nx, ny, len, g);
-            dot = F.x * mu.x + F.y * mu.y + F.z * mu.z + F.w * mu.w;
+            const d4 fR = face_state_used<LINEAR>(uR, gxR, gyR, __ldg(&gm[6]), __ldg(&gm[7]), g, wR, usedR);
             roe_flux_vjp(wL, wR, nx, ny, len, g, mu, bwL, bwR);
             to_prim_vjp(fR, wR, g, bwR, bfR);
             to_prim_vjp(fL, wL, g, bwL, bfL);
         } else {  // slip wall / symmetry: the ghost is a function of the L face state
             const d4 fR = ghost_slip(fL, wL, nx, ny);
             const Prim wR = to_prim(fR, g);
-            const d4 F = roe_flux(wL, wR, nx, ny, len, g);
-            dot = F.x * mu.x + F.y * mu.y + F.z * mu.z + F.w * mu.w;
             roe_flux_vjp(wL, wR, nx, ny, len, g, mu, bwL, bwR);
             d4 bgR = mk4(0, 0, 0, 0);
             to_prim_vjp(fR, wR, g, bwR, bgR);
             ghost_slip_vjp(fL, wL, nx, ny, bgR, bfL, bwL);
             to_prim_vjp(fL, wL, g, bwL, bfL);
         }
+        const int flag = (usedL ? 1 : 0) | (usedR ? 2 : 0);  // the L / R face state is the linear reconstruction
         aL[e] = bfL;
         aR[e] = bfR;
         aflag[e] = flag;
-    }
-    // deterministic block partial of sum_e F_e . mu_e
-    for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
-    __shared__ double sm[8];
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = dot;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sm[i];
-        dot_part[blockIdx.x] = s;
     }
 }
 
@@ -169,6 +152,7 @@ __global__ void __launch_bounds__(256) k_adj_cell(const d4* __restrict__ U, Mesh
             vx[j] = __ldg(&X[2 * j]);
             vy[j] = __ldg(&X[2 * j + 1]);
         }
+#pragma unroll
         for (int v = 0; v < 4; v++) {
             const double gx = fma(b0[2], dU[2][v], fma(b0[1], dU[1][v], b0[0] * dU[0][v]));
             const double gy = fma(b1[2], dU[2][v], fma(b1[1], dU[1][v], b1[0] * dU[0][v]));
@@ -185,13 +169,15 @@ __global__ void __launch_bounds__(256) k_adj_cell(const d4* __restrict__ U, Mesh
                 double d[3];
                 for (int j = 0; j < 3; j++) d[j] = fma(gx, vx[j], gy * vy[j]);
                 int jh = 0, jl = 0;
+                double dh = d[0], dl = d[0];
+#pragma unroll
                 for (int j = 1; j < 3; j++) {
-                    if (dlt(d[jh], d[j])) jh = j;
-                    if (dlt(d[j], d[jl])) jl = j;
+                    if (dlt(dh, d[j])) { dh = d[j]; jh = j; }
+                    if (dlt(d[j], dl)) { dl = d[j]; jl = j; }
                 }
-                const double dp = d[jh] + kEps, dn = d[jl] - kEps;
-                const bool lim_p = pos(d[jh]) && dlt(np, dp);
-                const bool lim_n = neg(d[jl]) && dlt(dn, nn);
+                const double dp = dh + kEps, dn = dl - kEps;
+                const bool lim_p = pos(dh) && dlt(np, dp);
+                const bool lim_n = neg(dl) && dlt(dn, nn);
                 if (lim_p || lim_n) {
                     const bool use_p = lim_p && (!lim_n || dlt(nn * dp, np * dn));
                     const double num = use_p ? np : nn, den = use_p ? dp : dn;
@@ -204,9 +190,14 @@ __global__ void __launch_bounds__(256) k_adj_cell(const d4* __restrict__ U, Mesh
                     bgy *= phi;
                     const double b_num = b_phi * rden;
                     const double b_den = -b_phi * phi * rden;
-                    bgx = fma(b_den, vx[jj], bgx);
-                    bgy = fma(b_den, vy[jj], bgy);
-                    if (kk >= 0) bd[kk][v] += b_num;
+                    // selects rather than vx[jj] / bd[kk][v]: keeps the arrays in registers
+                    const double vxj = jj == 0 ? vx[0] : (jj == 1 ? vx[1] : vx[2]);
+                    const double vyj = jj == 0 ? vy[0] : (jj == 1 ? vy[1] : vy[2]);
+                    bgx = fma(b_den, vxj, bgx);
+                    bgy = fma(b_den, vyj, bgy);
+#pragma unroll
+                    for (int k = 0; k < 3; k++)
+                        if (k == kk) bd[k][v] += b_num;
                 }
             }
             for (int k = 0; k < 3; k++)
@@ -217,55 +208,56 @@ __global__ void __launch_bounds__(256) k_adj_cell(const d4* __restrict__ U, Mesh
 }
 
 // ---- per cell: neighbours' LSQ adjoints and the stage's Runge-Kutta combination ------
-// U_s = a U_0 + b (U_in + dt R(U_in)):  lam_in = b (lam_s + dt J^T lam_s);  acc0 (+)= a lam_s
+// U_s = a U_0 + b (U_in + dt R(U_in)):  lam_in = b (lam_s + dt J^T lam_s);  acc0 (+)= a lam_s.
+// acc_mode 0: acc0 = a lam_s; 1: acc0 += a lam_s; 2: nothing; 3 (a = 0, the first stage, whose
+// input is U_0 itself): lam_in += acc0.  dot_part[block] = sum over the block's cells of
+// lam_s . R_s (= d loss / d dt through this stage, divided by b), summed in a fixed order.
 __global__ void __launch_bounds__(256) k_adj_combine(MeshView m, const int* __restrict__ rev,
                                                      const d4* __restrict__ lam_dir, const d4* __restrict__ bdU,
-                                                     const d4* __restrict__ lam_s, const double* __restrict__ dt_p,
-                                                     double a, double b, int acc_mode, d4* __restrict__ lam_in,
-                                                     d4* __restrict__ acc0, int linear) {
+                                                     const d4* __restrict__ lam_s, const d4* __restrict__ R_s,
+                                                     const double* __restrict__ dt_p, double a, double b,
+                                                     int acc_mode, d4* __restrict__ lam_in, d4* __restrict__ acc0,
+                                                     int linear, double* __restrict__ dot_part) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= m.N) return;
-    const d4 ld = ld4(&lam_dir[c]);
-    double r[4] = {ld.x, ld.y, ld.z, ld.w};
-    if (linear) {
-        const int nnb = __ldg(&m.c_nnb[c]);
-        for (int k = 0; k < nnb; k++) {
-            const d4 own = ld4(&bdU[(size_t)c * 3 + k]);  // d/dU_c of U_k - U_c
-            r[0] -= own.x; r[1] -= own.y; r[2] -= own.z; r[3] -= own.w;
-            const int q = __ldg(&m.c_nbr[c * 3 + k]);
-            const d4 other = ld4(&bdU[(size_t)q * 3 + __ldg(&rev[c * 3 + k])]);  // c is a neighbour of q
-            r[0] += other.x; r[1] += other.y; r[2] += other.z; r[3] += other.w;
+    double dot = 0.0;
+    if (c < m.N) {
+        const d4 ld = ld4(&lam_dir[c]);
+        double r[4] = {ld.x, ld.y, ld.z, ld.w};
+        if (linear) {
+            const int nnb = __ldg(&m.c_nnb[c]);
+            for (int k = 0; k < nnb; k++) {
+                const d4 own = ld4(&bdU[(size_t)c * 3 + k]);  // d/dU_c of U_k - U_c
+                r[0] -= own.x; r[1] -= own.y; r[2] -= own.z; r[3] -= own.w;
+                const int q = __ldg(&m.c_nbr[c * 3 + k]);
+                const d4 other = ld4(&bdU[(size_t)q * 3 + __ldg(&rev[c * 3 + k])]);  // c is a neighbour of q
+                r[0] += other.x; r[1] += other.y; r[2] += other.z; r[3] += other.w;
+            }
         }
+        const double dt = *dt_p;
+        const d4 ls = ld4(&lam_s[c]);
+        const d4 rs = ld4(&R_s[c]);
+        dot = fma(ls.x, rs.x, fma(ls.y, rs.y, fma(ls.z, rs.z, ls.w * rs.w)));
+        d4 li = mk4(b * fma(dt, r[0], ls.x), b * fma(dt, r[1], ls.y), b * fma(dt, r[2], ls.z), b * fma(dt, r[3], ls.w));
+        if (acc_mode == 0) {
+            acc0[c] = mk4(a * ls.x, a * ls.y, a * ls.z, a * ls.w);
+        } else if (acc_mode == 1) {
+            const d4 o = acc0[c];
+            acc0[c] = mk4(fma(a, ls.x, o.x), fma(a, ls.y, o.y), fma(a, ls.z, o.z), fma(a, ls.w, o.w));
+        } else if (acc_mode == 3) {
+            const d4 o = acc0[c];
+            li = mk4(o.x + li.x, o.y + li.y, o.z + li.z, o.w + li.w);
+        }
+        lam_in[c] = li;
     }
-    const double dt = *dt_p;
-    const d4 ls = ld4(&lam_s[c]);
-    lam_in[c] = mk4(b * fma(dt, r[0], ls.x), b * fma(dt, r[1], ls.y), b * fma(dt, r[2], ls.z), b * fma(dt, r[3], ls.w));
-    if (acc_mode == 0) acc0[c] = mk4(a * ls.x, a * ls.y, a * ls.z, a * ls.w);
-    else if (acc_mode == 1) {
-        const d4 o = acc0[c];
-        acc0[c] = mk4(fma(a, ls.x, o.x), fma(a, ls.y, o.y), fma(a, ls.z, o.z), fma(a, ls.w, o.w));
+    for (int o = 16; o > 0; o >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, o);
+    __shared__ double sm[8];
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = dot;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < 8; i++) t += sm[i];
+        dot_part[blockIdx.x] = t;
     }
-}
-
-// lam = acc0 + lam_in (the first stage's input is U_0 itself)
-__global__ void __launch_bounds__(256) k_adj_add(int N, const d4* __restrict__ acc0, d4* __restrict__ lam) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= N) return;
-    const d4 a = acc0[c], l = lam[c];
-    lam[c] = mk4(a.x + l.x, a.y + l.y, a.z + l.z, a.w + l.w);
-}
-
-// lambda_dt = sum over stages of b_s (F . mu)_s, partials summed in a fixed order
-__global__ void k_adj_lamdt(const double* __restrict__ part, int nb, int nstages, const double* __restrict__ bs,
-                            double* out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double t = 0.0;
-    for (int s = 0; s < nstages; s++) {
-        double x = 0.0;
-        for (int i = 0; i < nb; i++) x += part[(size_t)s * nb + i];
-        t = fma(bs[s], x, t);
-    }
-    *out = t;
 }
 
 // smallest cell index whose CFL vol / alpha equals the step's minimum
@@ -277,14 +269,32 @@ __global__ void __launch_bounds__(256) k_adj_argmin(MeshView m, const double* __
     if ((unsigned long long)__double_as_longlong(d) == *dtmin) atomicMin(out, c);
 }
 
-// dt = CFL vol_c / alpha_c at the minimising cell c: adds lambda_dt d(dt)/dU_0 to lam
-__global__ void k_adj_dt(const d4* __restrict__ U0, MeshView m, Gas g, double CFL, const int* cstar,
-                         const double* dt_info, const double* lamdt, d4* lam) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// lambda_dt = sum over stages of b_s (lam_s . R_s), the combine kernel's block partials
+// reduced in a fixed order (thread-strided sums, then a shared-memory tree); then thread 0 adds
+// lambda_dt d(dt)/dU_0 to lam, dt = CFL vol_c / alpha_c at the minimising cell c
+constexpr int kDtThreads = 256;
+__global__ void __launch_bounds__(kDtThreads) k_adj_dt(const double* __restrict__ part, int nb, int nstages,
+                                                       double b0, double b1, double b2, const d4* __restrict__ U0,
+                                                       MeshView m, Gas g, double CFL, const int* cstar,
+                                                       const double* dt_info, d4* lam) {
+    __shared__ double red[kDtThreads];
+    double lt = 0.0;
+    for (int st = 0; st < nstages; st++) {
+        double x = 0.0;
+        for (int i = threadIdx.x; i < nb; i += kDtThreads) x += part[(size_t)st * nb + i];
+        red[threadIdx.x] = x;
+        __syncthreads();
+        for (int w = kDtThreads / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        lt = fma(st == 0 ? b0 : (st == 1 ? b1 : b2), red[0], lt);
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
     const int c = *cstar;
     if (c < 0 || c >= m.N) return;
     if (dt_info[0] != dt_info[1]) return;  // clamped to the end time: dt does not depend on U
-    const double lt = *lamdt;
     if (lt == 0.0) return;
     double alpha = 0.0;
     for (int k = m.dt_ptr[c]; k < m.dt_ptr[c + 1]; k++) {
@@ -366,15 +376,18 @@ struct Adjoint {
     int K = 0, S = 0, nseg = 0, nst = 0;
     std::vector<void*> owned;
     std::vector<d4*> chk;          // U at the start of each segment
-    std::vector<double> chk_t;     // t at the start of each segment
+    double* d_chk_t = nullptr;     // t at the start of each segment
     std::vector<d4*> seg_states;   // per step of a segment: U_0, U_1, U_2
+    std::vector<d4*> seg_gx, seg_gy;  // per stage of a segment's steps: the limited gradients
+    std::vector<d4*> seg_R;           // per stage of a segment's steps: the residual R(U_in)
     double* d_seg_dt = nullptr;    // per step: dt, dt_raw
     int* d_seg_cstar = nullptr;    // per step: the minimising cell
     d4 *d_lam = nullptr, *d_lam_in = nullptr, *d_acc0 = nullptr, *d_aL = nullptr, *d_aR = nullptr;
     d4 *d_lamdir = nullptr, *d_bdU = nullptr, *d_keepU = nullptr;
     int *d_aflag = nullptr, *d_rlist = nullptr, *d_rev = nullptr;
-    double *d_dotp = nullptr, *d_lamdt = nullptr, *d_bs = nullptr;
+    double* d_dotp = nullptr;
     bool ready = false;
+    bool last_kept = false;  // the segment buffers hold the last segment's steps
     long long restricted_before = 0;
     double ms_fwd = 0, ms_bwd = 0;
 
@@ -429,17 +442,25 @@ struct Adjoint {
         AK(cudaMemcpyAsync(d_rlist, rlist.data(), sizeof(int) * E, cudaMemcpyHostToDevice, s->stream));
         AK(cudaMemcpyAsync(d_rev, rev.data(), sizeof(int) * 3 * (size_t)N, cudaMemcpyHostToDevice, s->stream));
         chk.assign(nseg, nullptr);
-        chk_t.assign(nseg, 0.0);
         for (int i = 0; i < nseg; i++)
             if ((rc = alloc(chk[i], N))) return rc;
+        if ((rc = alloc(d_chk_t, nseg))) return rc;
         seg_states.assign((size_t)S * nst, nullptr);
         for (auto& q : seg_states)
             if ((rc = alloc(q, N))) return rc;
-        const int nb = nblk(E, 256);
+        const bool linear = p.reconstruct == 3002;
+        seg_gx.assign(linear ? (size_t)S * nst : 0, nullptr);
+        seg_gy.assign(seg_gx.size(), nullptr);
+        for (size_t i = 0; i < seg_gx.size(); i++)
+            if ((rc = alloc(seg_gx[i], N)) || (rc = alloc(seg_gy[i], N))) return rc;
+        seg_R.assign((size_t)S * nst, nullptr);
+        for (auto& q : seg_R)
+            if ((rc = alloc(q, N))) return rc;
+        const int nb = nblk(N, 256);
         if ((rc = alloc(d_seg_dt, 2 * (size_t)S)) || (rc = alloc(d_seg_cstar, S)) || (rc = alloc(d_lam, N)) ||
             (rc = alloc(d_lam_in, N)) || (rc = alloc(d_acc0, N)) || (rc = alloc(d_aL, E)) || (rc = alloc(d_aR, E)) ||
             (rc = alloc(d_lamdir, N)) || (rc = alloc(d_keepU, N)) || (rc = alloc(d_bdU, 3 * (size_t)N)) || (rc = alloc(d_aflag, E)) ||
-            (rc = alloc(d_dotp, (size_t)nb * 3)) || (rc = alloc(d_lamdt, 1)) || (rc = alloc(d_bs, 3)))
+            (rc = alloc(d_dotp, (size_t)nb * 3)))
             return rc;
         return 0;
     }
@@ -460,41 +481,55 @@ struct Adjoint {
         dev::launch_dt_final(st, v.d_state, true);
         AK(cudaMemcpyAsync(d_seg_dt + 2 * slot, &v.d_state->dt, sizeof(double), cudaMemcpyDeviceToDevice, st));
         AK(cudaMemcpyAsync(d_seg_dt + 2 * slot + 1, &v.d_state->dt_raw, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        // each stage's gradients go to the segment's buffers (kept for the reverse sweep)
+        d4 *gx0 = v.d_Gx, *gy0 = v.d_Gy;
+        auto stage = [&](int si, int kind) {
+            if (!seg_gx.empty()) {
+                v.d_Gx = seg_gx[(size_t)slot * nst + si];
+                v.d_Gy = seg_gy[(size_t)slot * nst + si];
+            }
+            v.d_rec_R = seg_R[(size_t)slot * nst + si];
+            v.enqueue_stage(kind);
+        };
         if (v.p.time_advance == 3101) {
-            v.enqueue_stage(dev::STAGE_EULER);
+            stage(0, dev::STAGE_EULER);
         } else {
-            v.enqueue_stage(dev::STAGE_SSP_1);
+            stage(0, dev::STAGE_SSP_1);
             AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst + 1], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
-            v.enqueue_stage(dev::STAGE_SSP_2);
+            stage(1, dev::STAGE_SSP_2);
             AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst + 2], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
-            v.enqueue_stage(dev::STAGE_SSP_3);
+            stage(2, dev::STAGE_SSP_3);
         }
+        v.d_Gx = gx0;
+        v.d_Gy = gy0;
+        v.d_rec_R = nullptr;
         dev::launch_restrict(st, v.d_U, v.mv, v.d_cell_ref, v.d_cell_new, v.d_flags, v.d_flag_count, Solver::kFlagCap,
                              v.p.restrict_ref, v.gas, v.d_status);
         AK(cudaGetLastError());
         return 0;
     }
 
-    // one stage VJP: lam_s (d_lam) -> lam_in (d_lam_in), acc0, partial F.mu in dot slot
-    int stage_vjp(const d4* Uin, const double* dt_p, double a, double b, int acc_mode, int dot_slot) {
+    // one stage VJP: lam_s (d_lam) -> lam_in (d_lam_in), acc0, partial F.mu in dot slot;
+    // (Uin, Gx, Gy): the stage's input state and the limited gradients the forward used
+    int stage_vjp(const d4* Uin, const d4* Gx, const d4* Gy, const d4* Rs, const double* dt_p, double a, double b,
+                  int acc_mode, int dot_slot) {
         Solver& v = *s;
         cudaStream_t st = v.stream;
         const bool linear = v.p.reconstruct == 3002;
-        if (linear) dev::launch_grad(st, 1, v.p.limiter == 1, Uin, v.mv, v.d_Gx, v.d_Gy);
-        const int nbE = nblk(v.E, 256), nbN = nblk(v.N, 256);
-        double* dp = d_dotp + (size_t)dot_slot * nbE;
+        const int nbE = nblk(v.E, dev::kEdgeThreads), nbN = nblk(v.N, 256);
+        double* dp = d_dotp + (size_t)dot_slot * nbN;
         if (linear)
-            dev::k_adj_edge<true><<<nbE, 256, 0, st>>>(Uin, v.d_Gx, v.d_Gy, v.mv, v.gas, d_lam, d_rlist, d_aL, d_aR,
-                                                       d_aflag, dp);
+            dev::k_adj_edge<true><<<nbE, dev::kEdgeThreads, 0, st>>>(Uin, Gx, Gy, v.mv, v.gas, d_lam, d_rlist, d_aL,
+                                                                     d_aR, d_aflag);
         else
-            dev::k_adj_edge<false><<<nbE, 256, 0, st>>>(Uin, v.d_Gx, v.d_Gy, v.mv, v.gas, d_lam, d_rlist, d_aL, d_aR,
-                                                        d_aflag, dp);
+            dev::k_adj_edge<false><<<nbE, dev::kEdgeThreads, 0, st>>>(Uin, Gx, Gy, v.mv, v.gas, d_lam, d_rlist, d_aL,
+                                                                      d_aR, d_aflag);
         if (!linear) dev::k_adj_cell<false, false><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, d_aflag, d_lamdir, d_bdU);
         else if (v.p.limiter == 1)
             dev::k_adj_cell<true, true><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, d_aflag, d_lamdir, d_bdU);
         else dev::k_adj_cell<true, false><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, d_aflag, d_lamdir, d_bdU);
-        dev::k_adj_combine<<<nbN, 256, 0, st>>>(v.mv, d_rev, d_lamdir, d_bdU, d_lam, dt_p, a, b, acc_mode, d_lam_in,
-                                                d_acc0, linear ? 1 : 0);
+        dev::k_adj_combine<<<nbN, 256, 0, st>>>(v.mv, d_rev, d_lamdir, d_bdU, d_lam, Rs, dt_p, a, b, acc_mode,
+                                                d_lam_in, d_acc0, linear ? 1 : 0, dp);
         AK(cudaGetLastError());
         return 0;
     }
@@ -504,35 +539,55 @@ struct Adjoint {
         Solver& v = *s;
         cudaStream_t st = v.stream;
         const double* dtp = d_seg_dt + 2 * slot;
-        const int nbN = nblk(v.N, 256), nbE = nblk(v.E, 256);
+        const int nbN = nblk(v.N, 256);
+        auto R = [&](int si) { return seg_R[(size_t)slot * nst + si]; };
+        auto gx = [&](int si) { return seg_gx.empty() ? v.d_Gx : seg_gx[(size_t)slot * nst + si]; };
+        auto gy = [&](int si) { return seg_gy.empty() ? v.d_Gy : seg_gy[(size_t)slot * nst + si]; };
         int rc;
+        double b0 = 1.0, b1 = 0.0, b2 = 0.0;  // b_s of the stages in reverse order
         if (v.p.time_advance == 3101) {
             // U1 = U0 + dt R(U0): a = 0, b = 1
-            if ((rc = stage_vjp(seg_states[(size_t)slot], dtp, 0.0, 1.0, 2, 0))) return rc;
-            const double bs[3] = {1.0, 0.0, 0.0};
-            AK(cudaMemcpyAsync(d_bs, bs, sizeof bs, cudaMemcpyHostToDevice, st));
+            if ((rc = stage_vjp(seg_states[(size_t)slot], gx(0), gy(0), R(0), dtp, 0.0, 1.0, 2, 0))) return rc;
             std::swap(d_lam, d_lam_in);
         } else {
             const d4* U0 = seg_states[(size_t)slot * 3];
             const d4* U1 = seg_states[(size_t)slot * 3 + 1];
             const d4* U2 = seg_states[(size_t)slot * 3 + 2];
             // U3 = 1/3 U0 + 2/3 (U2 + dt R(U2))
-            if ((rc = stage_vjp(U2, dtp, 1.0 / 3.0, 2.0 / 3.0, 0, 0))) return rc;
+            if ((rc = stage_vjp(U2, gx(2), gy(2), R(2), dtp, 1.0 / 3.0, 2.0 / 3.0, 0, 0))) return rc;
             std::swap(d_lam, d_lam_in);
             // U2 = 3/4 U0 + 1/4 (U1 + dt R(U1))
-            if ((rc = stage_vjp(U1, dtp, 0.75, 0.25, 1, 1))) return rc;
+            if ((rc = stage_vjp(U1, gx(1), gy(1), R(1), dtp, 0.75, 0.25, 1, 1))) return rc;
             std::swap(d_lam, d_lam_in);
-            // U1 = U0 + dt R(U0)
-            if ((rc = stage_vjp(U0, dtp, 0.0, 1.0, 2, 2))) return rc;
+            // U1 = U0 + dt R(U0); U0 also feeds stages 2 and 3 directly (acc0)
+            if ((rc = stage_vjp(U0, gx(0), gy(0), R(0), dtp, 0.0, 1.0, 3, 2))) return rc;
             std::swap(d_lam, d_lam_in);
-            dev::k_adj_add<<<nbN, 256, 0, st>>>(v.N, d_acc0, d_lam);
-            const double bs[3] = {2.0 / 3.0, 0.25, 1.0};
-            AK(cudaMemcpyAsync(d_bs, bs, sizeof bs, cudaMemcpyHostToDevice, st));
+            b0 = 2.0 / 3.0;
+            b1 = 0.25;
+            b2 = 1.0;
         }
-        dev::k_adj_lamdt<<<1, 32, 0, st>>>(d_dotp, nbE, nst, d_bs, d_lamdt);
-        dev::k_adj_dt<<<1, 32, 0, st>>>(seg_states[(size_t)slot * nst], v.mv, v.gas, v.p.CFL, d_seg_cstar + slot, dtp,
-                                        d_lamdt, d_lam);
+        dev::k_adj_dt<<<1, dev::kDtThreads, 0, st>>>(d_dotp, nbN, nst, b0, b1, b2, seg_states[(size_t)slot * nst],
+                                                    v.mv, v.gas, v.p.CFL, d_seg_cstar + slot, dtp, d_lam);
         AK(cudaGetLastError());
+        return 0;
+    }
+
+    // the state and time at the start of segment i
+    int load_segment(int i) {
+        Solver& v = *s;
+        AK(cudaMemcpyAsync(v.d_U, chk[i], sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, v.stream));
+        AK(cudaMemcpyAsync(&v.d_state->t, d_chk_t + i, sizeof(double), cudaMemcpyDeviceToDevice, v.stream));
+        return 0;
+    }
+
+    // runs segment i's steps kernel by kernel, keeping each step's states (record_step)
+    int record_segment(int i) {
+        Solver& v = *s;
+        AK(cudaMemcpyAsync(&v.d_state->T, &v.p.T_end, sizeof(double), cudaMemcpyHostToDevice, v.stream));
+        const int n = std::min(S, K - i * S);
+        int rc;
+        for (int k = 0; k < n; k++)
+            if ((rc = record_step(k))) return rc;
         return 0;
     }
 
@@ -553,11 +608,13 @@ struct Adjoint {
         AK(cudaEventRecord(a, v.stream));
         for (int i = 0; i < nseg; i++) {
             AK(cudaMemcpyAsync(chk[i], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, v.stream));
-            double t;
-            if ((rc = v.get_time(&t, nullptr))) return rc;
-            chk_t[i] = t;
+            AK(cudaMemcpyAsync(d_chk_t + i, &v.d_state->t, sizeof(double), cudaMemcpyDeviceToDevice, v.stream));
             const int n = std::min(S, K - i * S);
-            if ((rc = v.step_async(v.p.T_end, n))) return rc;
+            if (i + 1 < nseg) {
+                if ((rc = v.step_async(v.p.T_end, n))) return rc;
+            } else if ((rc = record_segment(i))) {  // the reverse sweep starts here: keep its states now
+                return rc;
+            }
         }
         AK(cudaEventRecord(b, v.stream));
         AK(cudaEventSynchronize(b));
@@ -568,6 +625,7 @@ struct Adjoint {
         cudaEventDestroy(b);
         if ((rc = v.check_status())) return rc;
         if (UK && (rc = v.get_state(UK))) return rc;
+        last_kept = true;
         ready = true;
         return 0;
     }
@@ -589,15 +647,13 @@ struct Adjoint {
         AK(cudaEventCreate(&b));
         AK(cudaEventRecord(a, st));
         for (int i = nseg - 1; i >= 0; i--) {
-            AK(cudaMemcpyAsync(v.d_U, chk[i], sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
-            if ((rc = v.set_time(chk_t[i]))) return rc;
-            AK(cudaMemcpyAsync(&v.d_state->T, &v.p.T_end, sizeof(double), cudaMemcpyHostToDevice, st));
+            // the last segment's states are still those the forward sweep recorded
+            if ((i + 1 < nseg || !last_kept) && ((rc = load_segment(i)) || (rc = record_segment(i)))) return rc;
             const int n = std::min(S, K - i * S);
-            for (int k = 0; k < n; k++)
-                if ((rc = record_step(k))) return rc;
             for (int k = n - 1; k >= 0; k--)
                 if ((rc = step_vjp(k))) return rc;
         }
+        last_kept = nseg == 1;
         AK(cudaEventRecord(b, st));
         AK(cudaEventSynchronize(b));
         float ms = 0;

@@ -176,6 +176,25 @@ __device__ __forceinline__ void roe_flux_vjp(const Prim& L, const Prim& R, doubl
     bR.r = b_Rr; bR.u = b_Ru; bR.v = b_Rv; bR.p = b_Rp; bR.ir = b_Rir;
 }
 
+// face_state (step_device.cuh) that also reports whether the linear reconstruction was kept
+template <bool LINEAR>
+__device__ __forceinline__ d4 face_state_used(const d4 u, const d4 gx, const d4 gy, double dx, double dy,
+                                              const Gas& g, Prim& w, bool& used) {
+    used = false;
+    if (!LINEAR) {
+        w = to_prim(u, g);
+        return u;
+    }
+    const d4 f = lin(u, gx, gy, dx, dy);
+    w = to_prim(f, g);
+    if (out_of_range(w.r, w.p)) {
+        w = to_prim(u, g);
+        return u;
+    }
+    used = true;
+    return f;
+}
+
 // adjoint of ghost_slip (physics.cuh): bUR -> bUL (ghost_slip reads UL.x, UL.w and the
 // primitive velocity of UL)
 __device__ __forceinline__ void ghost_slip_vjp(const d4 UL, const Prim& wL, double nx, double ny, const d4 bUR,

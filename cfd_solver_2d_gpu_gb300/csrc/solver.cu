@@ -227,7 +227,7 @@ void Solver::enqueue_stage(int kind) {
     launches += (mv.E_int > 0) + (mv.E > mv.E_int);
     mark(PROF_UPDATE, true);
     dev::launch_update(s, kind, d_U, d_U0, d_K1, d_rhs, d_F, mv, d_state, gas, d_flags, d_flag_count, kFlagCap,
-                       d_status);
+                       d_status, d_rec_R);
     mark(PROF_UPDATE, false);
     launches += 1;
 }

@@ -302,7 +302,8 @@ template <int KIND>
 __device__ __forceinline__ void update_cell(int c, d4* __restrict__ U, const d4* __restrict__ U0, d4* __restrict__ K1,
                                             d4* __restrict__ rhs_out, const d4* __restrict__ F, const MeshView& m,
                                             double dt, double dt6, const Gas& g, int* __restrict__ flag_list,
-                                            unsigned int* flag_count, int flag_cap, Status* st) {
+                                            unsigned int* flag_count, int flag_cap, Status* st,
+                                            d4* __restrict__ rec_R = nullptr) {
     const int r0 = __ldg(&m.c_edge[c * 3]);
     const d4 f0 = ld4(&F[r0 >= 0 ? r0 : ~r0]);
     d4 acc = (r0 >= 0) ? f0 : mk4(-f0.x, -f0.y, -f0.z, -f0.w);  // 0 + s f0 == s f0
@@ -315,6 +316,7 @@ __device__ __forceinline__ void update_cell(int c, d4* __restrict__ U, const d4*
     }
     const double mv = __ldg(&m.c_mvol[c]);
     const d4 k = mk4(mv * acc.x, mv * acc.y, mv * acc.z, mv * acc.w);
+    if (rec_R) rec_R[c] = k;  // the stage's residual, kept for the adjoint
     if (KIND == STAGE_RHS) {
         rhs_out[c] = k;
         return;

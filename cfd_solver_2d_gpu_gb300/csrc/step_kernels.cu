@@ -86,7 +86,8 @@ template <int KIND>
 __global__ void __launch_bounds__(256) k_update(d4* __restrict__ U, const d4* __restrict__ U0, d4* __restrict__ K1,
                                                 d4* __restrict__ rhs_out, const d4* __restrict__ F, MeshView m,
                                                 const StepState* s, Gas g, int* __restrict__ flag_list,
-                                                unsigned int* flag_count, int flag_cap, Status* st) {
+                                                unsigned int* flag_count, int flag_cap, Status* st,
+                                                d4* __restrict__ rec_R) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
     double dt = 0.0, dt6 = 0.0;
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(256) k_update(d4* __restrict__ U, const d4* __
         dt = s->dt;
         dt6 = s->dt6;
     }
-    update_cell<KIND>(c, U, U0, K1, rhs_out, F, m, dt, dt6, g, flag_list, flag_count, flag_cap, st);
+    update_cell<KIND>(c, U, U0, K1, rhs_out, F, m, dt, dt6, g, flag_list, flag_count, flag_cap, st, rec_R);
 }
 
 __global__ void k_restrict(d4* U, MeshView m, const int* __restrict__ cell_ref_of_dev,
@@ -231,10 +232,11 @@ void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, 
 
 void launch_update(cudaStream_t s, int kind, d4* U, const d4* U0, d4* K1, d4* rhs,
                    const d4* F, const MeshView& m, const StepState* st, const Gas& g, int* flag_list,
-                   unsigned int* flag_count, int flag_cap, Status* status) {
+                   unsigned int* flag_count, int flag_cap, Status* status, d4* rec_R) {
     if (m.N <= 0) return;
     const int b = blocks(m.N, 256);
-#define FVGB_UPD(K) k_update<K><<<b, 256, 0, s>>>(U, U0, K1, rhs, F, m, st, g, flag_list, flag_count, flag_cap, status)
+#define FVGB_UPD(K) \
+    k_update<K><<<b, 256, 0, s>>>(U, U0, K1, rhs, F, m, st, g, flag_list, flag_count, flag_cap, status, rec_R)
     switch (kind) {
     case STAGE_RHS: FVGB_UPD(STAGE_RHS); break;
     case STAGE_EULER: FVGB_UPD(STAGE_EULER); break;

@@ -6,7 +6,15 @@ torch.autograd.Function wrapper.
 
 Loss: L = 1/2 sum_c (rho_K(c) - rho_target(c))^2, the target being the
 forward solution from a perturbed initial state (vortex strength and centre
-shifted by seeded amounts)."""
+shifted by seeded amounts).
+
+The forward map is only piecewise smooth: the Barth limiter's min(1, .) and
+its choice of vertex, and the argmin cell of the global time step, switch
+branch where two candidates tie. The isentropic vortex is uniform to ~1e-11
+away from its core and a regular mesh gives equal time steps in many cells,
+so a finite-difference step of 1e-6 crosses branches there and the difference
+quotient is no derivative. The test states therefore carry a smooth wave on
+top of the vortex everywhere, and the meshes are jittered."""
 import numpy as np
 import pytest
 
@@ -31,13 +39,13 @@ def setup_case(tmp_path, n=24, jitter=0.2, time_advance=3104, reconstruct=3002, 
     p = fv.Params.from_toml(tp)
     mesh = fv.Mesh.read_su2(su2, p)
     solver = fv.GPUSolver2(mesh, p)
-    U0 = solver.get_state()
+    U0 = cases.wavy(mesh, solver.get_state())
     # target: vortex strength 5 (1 + 0.02 r1), centre (5 + 0.1 r2, 5 + 0.1 r3)
     rng = np.random.default_rng(7)
     r = rng.uniform(-1, 1, 3)
     pt = fv.Params.from_toml(tp)
     pt.vortex[0], pt.vortex[1], pt.vortex[2] = 5 + 0.1 * r[1], 5 + 0.1 * r[2], 5 * (1 + 0.02 * r[0])
-    Ut0 = fv.initial_field(mesh, pt)
+    Ut0 = cases.wavy(mesh, fv.initial_field(mesh, pt))
     return tp, su2, p, mesh, solver, U0, Ut0
 
 
@@ -80,8 +88,7 @@ def test_adjoint_matches_fd_second_order_ssp(tmp_path):
 
 
 def test_adjoint_matches_fd_first_order_euler(tmp_path):
-    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=16, jitter=0.0, time_advance=3101, reconstruct=3001,
-                                                   CFL=0.5)
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=16, time_advance=3101, reconstruct=3001, CFL=0.5)
     K = 8
     rho_t = forward(solver, p, Ut0, K)[0]
     errs, _ = fd_check(solver, p, U0, rho_t, K, 6)
