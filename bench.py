@@ -436,12 +436,13 @@ def main():
                 "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": algo[dom], "avg_launch_ms": avg_ms,
                 "share_of_step": prof[dom][0] / sum(v[0] for v in prof.values())}
-        fp64_peak = 1207.0  # GFLOP/s, FP64 FMA chain measured on this machine's GB300 (profiles/fp64_peak.txt)
+        fp64_peak = fv.fp64_peak(local)  # GFLOP/s, register FMA chains on every SM, measured now
         fp64 = None
         if ncu.get(dom, {}).get("fp64_flop_per_launch"):
             a64 = ncu[dom]["fp64_flop_per_launch"] / (avg_ms / 1e3) / 1e9
             fp64 = {"achieved_gflops": a64, "peak_gflops": fp64_peak, "frac": a64 / fp64_peak,
-                    "kernel": dom, "source": "fp64 flop per launch from ncu x live launch time"}
+                    "kernel": dom, "peak_source": "fvgb_fp64_peak (FMA chains, measured in this run)",
+                    "source": "fp64 flop per launch from ncu x live launch time"}
         stage_roof = {"achieved": stage_bytes(N, E, V) / (stage_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                       "frac": stage_bytes(N, E, V) / (stage_ms / 1e3) / 1e9 / peak,
                       "bytes_per_stage": stage_bytes(N, E, V), "formula": "332N + 48E + 16V"}

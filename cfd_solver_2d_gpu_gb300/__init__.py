@@ -117,6 +117,7 @@ def lib():
             "fvgb_batch_step_timed": (i, [v, i, dp]),
             "fvgb_batch_tune": (i, [v, i, c, i]),
             "fvgb_batch_info": (i, [v, ctypes.POINTER(ctypes.c_longlong)]),
+            "fvgb_fp64_peak": (i, [i, dp]),
             "fvgb_last_error": (c, []),
             "fvgb_version": (c, []),
         }
@@ -178,6 +179,13 @@ class Mesh:
         n = int(np.prod(shape))
         ptr = ctypes.cast(getattr(self.soa, name), ctypes.POINTER(ct * n))
         return np.frombuffer(ptr.contents, dtype=np.float64 if code == "d" else np.int32).reshape(shape).copy()
+
+
+def fp64_peak(device=0):
+    """The device's FP64 rate in GFLOP/s (FMA = 2 flops), measured now (fvgb_fp64_peak)."""
+    g = ctypes.c_double()
+    _check(lib().fvgb_fp64_peak(int(device), ctypes.byref(g)))
+    return g.value
 
 
 def initial_field(mesh, params):

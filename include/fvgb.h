@@ -218,6 +218,12 @@ int fvgb_batch_info(fvgb_batch* b, long long out[8]);
 int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params* p, const double* U_dev, double* rhs_dev,
                      void* stream);
 
+/* No counterpart in the reference.  The device's FP64 arithmetic rate in
+ * GFLOP/s (an FMA counts two), measured with independent register FMA chains
+ * on every SM (best of three timed launches): the roofline denominator for
+ * kernels bound by the FP64 pipe. */
+int fvgb_fp64_peak(int device, double* gflops);
+
 const char* fvgb_last_error(void);
 const char* fvgb_version(void);
 
