@@ -89,6 +89,11 @@ def lib():
             "fvgb_write_su2_periodic_square": (i, [c, i, d, d, ctypes.c_ulonglong]),
             "fvgb_write_su2_cylinder": (i, [c, i, i, d, d, d]),
             "fvgb_initial_field": (i, [ctypes.POINTER(MeshSoA), v, dp]),
+            "fvgb_read_continue": (i, [c, i, ctypes.POINTER(v), dp, ip, dp]),
+            "fvgb_continue_state": (i, [v, dp]),
+            "fvgb_write_continue": (i, [v, c, d, i, d, dp]),
+            "fvgb_find_continue_file": (i, [c, c, c, i]),
+            "fvgb_run_config_read_toml": (i, [c, v]),
             "fvgb_create": (i, [ctypes.POINTER(MeshSoA), v, ctypes.POINTER(v)]),
             "fvgb_destroy": (None, [v]),
             "fvgb_set_state": (i, [v, dp]),
@@ -161,6 +166,26 @@ class Mesh:
         _check(lib().fvgb_mesh_read_su2(os.fsencode(path), int(eq), float(sc), ctypes.byref(ptr)))
         return cls(ptr)
 
+    @classmethod
+    def read_continue(cls, path, params=None, equation=None):
+        """A continue (pause_*.dat) file: returns (mesh, U[4][N], t, istep, CFL or None)."""
+        eq = equation if equation is not None else (params.equation if params is not None else 1)
+        ptr = ctypes.c_void_p()
+        t, istep, cfl = ctypes.c_double(), ctypes.c_int(), ctypes.c_double()
+        _check(lib().fvgb_read_continue(os.fsencode(path), int(eq), ctypes.byref(ptr), ctypes.byref(t),
+                                        ctypes.byref(istep), ctypes.byref(cfl)))
+        mesh = cls(ptr)
+        U = np.empty((4, mesh.N))
+        _check(lib().fvgb_continue_state(mesh._ptr, _dp(U)))
+        return mesh, U, t.value, istep.value, (cfl.value if cfl.value >= 0 else None)
+
+    def write_continue(self, path, U, t, istep, cfl):
+        """FieldWriter::writeContinueFile_1's format, 17 significant digits."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != (4, self.N):
+            raise ValueError(f"U must be (4, {self.N})")
+        _check(lib().fvgb_write_continue(self._ptr, os.fsencode(path), float(t), int(istep), float(cfl), _dp(U)))
+
     def __del__(self):
         if getattr(self, "_ptr", None):
             lib().fvgb_mesh_free(self._ptr)
@@ -179,6 +204,35 @@ class Mesh:
         n = int(np.prod(shape))
         ptr = ctypes.cast(getattr(self.soa, name), ctypes.POINTER(ct * n))
         return np.frombuffer(ptr.contents, dtype=np.float64 if code == "d" else np.int32).reshape(shape).copy()
+
+
+class RunConfig(ctypes.Structure):
+    """fvgb_run_config (include/fvgb.h): the driver loop's keys of input.toml."""
+    _fields_ = [("continue_run", ctypes.c_int), ("step_per_print", ctypes.c_int),
+                ("step_per_output_field", ctypes.c_int), ("step_per_output_hist", ctypes.c_int),
+                ("start_output_field", ctypes.c_int), ("max_iteration", ctypes.c_int),
+                ("tolerance_residual", ctypes.c_double), ("filename", ctypes.c_char * 256),
+                ("mesh_file_type", ctypes.c_char * 16)]
+
+
+def run_config(path):
+    """The driver's keys of input.toml (fvgb_run_config_read_toml) as a dict."""
+    c = RunConfig()
+    _check(lib().fvgb_run_config_read_toml(os.fsencode(path), ctypes.byref(c)))
+    out = {name: getattr(c, name) for name, _ in RunConfig._fields_}
+    out["filename"] = c.filename.decode()
+    out["mesh_file_type"] = c.mesh_file_type.decode()
+    return out
+
+
+def find_continue_file(directory, name):
+    """The newest pause_<name>[n].dat in directory (largest n > 0), or None."""
+    buf = ctypes.create_string_buffer(4096)
+    rc = lib().fvgb_find_continue_file(os.fsencode(directory), os.fsencode(name), buf, 4096)
+    if rc == -2:  # FVGB_ERR_IO: none there
+        return None
+    _check(rc)
+    return os.fsdecode(buf.value)
 
 
 def fp64_peak(device=0):

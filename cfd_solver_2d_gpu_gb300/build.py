@@ -1,6 +1,7 @@
 """Builds libfvgb.so in-tree: every csrc/*.cu and csrc/*.cpp compiled for
 sm_103a with nvcc (translation units in parallel), linked as one shared
-library next to this file."""
+library next to this file; then the headless driver fvgb_run
+(csrc/driver/fvgb_run.cpp, host C++ over the C ABI) next to it."""
 import concurrent.futures as cf
 import os
 import subprocess
@@ -11,6 +12,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfvgb.so")
+DRIVER_SRC = os.path.join(CSRC, "driver", "fvgb_run.cpp")
+DRIVER = os.path.join(HERE, "fvgb_run")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,6 +41,7 @@ def build(verbose=False, force=False):
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "fvgb.h"))
     if not force and not _stale(LIB, srcs + headers + [__file__]):
+        build_driver(force)
         return LIB
     common = [nvcc(), "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
               "-I", os.path.join(ROOT, "include"), "-I", CSRC] + ARCH
@@ -62,7 +66,24 @@ def build(verbose=False, force=False):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver(True)
     return LIB
+
+
+def build_driver(force=False):
+    """fvgb_run: the driver loop over the C ABI, linked against libfvgb.so (rpath $ORIGIN)."""
+    header = os.path.join(ROOT, "include", "fvgb.h")
+    if not force and not _stale(DRIVER, [DRIVER_SRC, header, LIB]):
+        return DRIVER
+    cxx = os.environ.get("CXX", "g++")
+    tmp = DRIVER + ".tmp"
+    cmd = [cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), DRIVER_SRC, "-o", tmp,
+           "-L", HERE, "-lfvgb", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stderr}")
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":

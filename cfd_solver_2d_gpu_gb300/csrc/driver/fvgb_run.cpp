@@ -1,0 +1,198 @@
+// fvgb_run: the headless driver loop over the C ABI, in place of
+// U2NITS::CDriver::start (FVMR/src/drivers/CDriver.cpp:31-184) for the GPU step.
+//
+//   fvgb_run input.toml [--output DIR] [--device N] [--quiet]
+//
+// Reads input.toml (fvgb_params_read_toml, fvgb_run_config_read_toml); the mesh
+// is <folder of input.toml>/<basic.filename>.su2.  With basic.continue it
+// restarts from the newest pause_<filename>[n].dat in the output folder (the
+// reference's rule, ContinueFileReader.cpp:24-53), else it starts from the
+// initial field.  The loop follows CDriver::start and its signal packs
+// (CDriver.cpp:202-263):
+//   - print the residual at step 1 and every output.step_per_print steps;
+//   - append a line to <filename>_hist.dat at step 1 and every
+//     output.step_per_output_hist steps;
+//   - stop at output.maxIteration, when the residual of rho falls to 1e-10
+//     (U2NITS::Math::EPSILON), when the time reaches max_physical_time, or on
+//     NaN; write pause_<filename>[istep].dat (istep as %04d) at the stop, or
+//     nan_<filename>[istep].dat after a NaN.
+// Between those events the device advances without host synchronisation
+// (fvgb_step over the whole span).  Differences from the reference:
+//   - The reference clamps dt so that t lands on T exactly and then keeps
+//     stepping with dt = 0 until maxIteration. This driver stops at the first
+//     output event at which t has reached T.
+//   - Continue files carry 17 significant digits (the reference's 6).
+//   - The hist file holds iteration, t and the four residuals.
+// Exit status: 0 at a normal stop, 2 after NaN or an out-of-range state,
+// 1 on any other error.
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fvgb.h"
+
+namespace {
+
+int report(const char* what) {
+    std::fprintf(stderr, "fvgb_run: %s: %s\n", what, fvgb_last_error());
+    return 1;
+}
+
+std::string folder_of(const std::string& path) {
+    const size_t k = path.find_last_of('/');
+    return k == std::string::npos ? std::string(".") : path.substr(0, k);
+}
+
+std::string step_tag(int istep) {
+    char b[32];
+    std::snprintf(b, sizeof b, "[%04d]", istep);  // COutput::updateFileName, FVMR/src/output/COutput.cpp:13-15
+    return b;
+}
+
+int usage() {
+    std::fprintf(stderr, "usage: fvgb_run input.toml [--output DIR] [--device N] [--quiet]\n");
+    return 1;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 2 || !std::strcmp(argv[1], "--help") || !std::strcmp(argv[1], "-h")) return usage();
+    const std::string toml = argv[1];
+    std::string out_dir = folder_of(toml) + "/output";
+    int device = -1;
+    bool quiet = false;
+    for (int i = 2; i < argc; i++) {
+        if (!std::strcmp(argv[i], "--output") && i + 1 < argc) out_dir = argv[++i];
+        else if (!std::strcmp(argv[i], "--device") && i + 1 < argc) device = std::atoi(argv[++i]);
+        else if (!std::strcmp(argv[i], "--quiet")) quiet = true;
+        else return usage();
+    }
+
+    fvgb_params p;
+    fvgb_run_config rc;
+    char mesh_name[512];
+    if (fvgb_params_read_toml(toml.c_str(), &p, mesh_name, sizeof mesh_name)) return report(toml.c_str());
+    if (fvgb_run_config_read_toml(toml.c_str(), &rc)) return report(toml.c_str());
+    if (device >= 0) p.device = device;
+    if (std::strcmp(rc.mesh_file_type, "su2") != 0) {
+        std::fprintf(stderr, "fvgb_run: basic.meshFileType = \"%s\": only su2 meshes are read\n", rc.mesh_file_type);
+        return 1;
+    }
+    mkdir(out_dir.c_str(), 0755);
+    const std::string name = rc.filename;
+
+    // CInput::readField_1 (FVMR/src/input/CInput.cpp:102-120)
+    fvgb_mesh* mesh = nullptr;
+    std::vector<double> U;
+    double t = 0.0;
+    int istep = 0;
+    bool restarted = false;
+    if (rc.continue_run) {
+        char path[4096];
+        if (fvgb_find_continue_file(out_dir.c_str(), name.c_str(), path, sizeof path) == 0) {
+            double cfl = -1.0;
+            if (fvgb_read_continue(path, p.equation, &mesh, &t, &istep, &cfl)) return report(path);
+            if (cfl >= 0.0) p.CFL = cfl;  // ContinueFileReader.cpp:98-100 keeps the saved CFL
+            fvgb_mesh_soa soa;
+            fvgb_mesh_view(mesh, &soa);
+            U.resize(4 * (size_t)soa.num_element);
+            if (fvgb_continue_state(mesh, U.data())) return report(path);
+            restarted = true;
+            if (!quiet) std::printf("continue from: %s (step %d, t = %.17g)\n", path, istep, t);
+        } else if (!quiet) {
+            std::printf("failed to read continue file (pause_*.dat), will read mesh file.\n");
+        }
+    }
+    fvgb_mesh_soa soa;
+    if (!restarted) {
+        const std::string su2 = folder_of(toml) + "/" + name + ".su2";
+        if (fvgb_mesh_read_su2(su2.c_str(), p.equation, p.mesh_scale, &mesh)) return report(su2.c_str());
+        fvgb_mesh_view(mesh, &soa);
+        U.resize(4 * (size_t)soa.num_element);
+        if (fvgb_initial_field(&soa, &p, U.data())) return report("initial field");
+    } else {
+        fvgb_mesh_view(mesh, &soa);
+    }
+
+    fvgb_handle* h = nullptr;
+    if (fvgb_create(&soa, &p, &h)) return report("fvgb_create");
+    if (fvgb_set_state(h, U.data())) return report("fvgb_set_state");
+
+    const std::string hist_path = out_dir + "/" + name + "_hist.dat";
+    FILE* hist = std::fopen(hist_path.c_str(), restarted ? "a" : "w");
+    if (!hist) {
+        std::fprintf(stderr, "fvgb_run: cannot write %s\n", hist_path.c_str());
+        return 1;
+    }
+    if (!restarted) std::fprintf(hist, "VARIABLES = \"Iteration\" \"Time\" \"Residual_rho\" \"Residual_rhou\" "
+                                       "\"Residual_rhov\" \"Residual_rhoE\"\n");
+
+    const double T = p.T_end;
+    const int max_it = rc.max_iteration;
+    const double kEpsilon = 1e-10;  // U2NITS::Math::EPSILON, FVMR/src/math/CommonValue.h
+    int status = 0;
+    const char* why = "maximum iteration reached";
+    std::string final_prefix = "pause_";
+    auto next_multiple = [](int after, int every) { return (after / every + 1) * every; };
+    while (istep < max_it) {
+        // the next step at which CDriver::start would print or write (modifySignalPack1_output)
+        int target = max_it;
+        if (istep == 0) target = 1;
+        target = std::min(target, next_multiple(istep, rc.step_per_print));
+        target = std::min(target, next_multiple(istep, rc.step_per_output_hist));
+        int rcs = fvgb_step(h, &t, T, target - istep);
+        if (rcs == FVGB_ERR_NAN || rcs == FVGB_ERR_RANGE) {
+            std::fprintf(stderr, "fvgb_run: %s near step %d\n", fvgb_last_error(), target);
+            istep = target;
+            status = 2;
+            why = "NaN or out-of-range state detected";
+            final_prefix = "nan_";
+            break;
+        }
+        if (rcs) return report("fvgb_step");
+        istep = target;
+        double res[4];
+        if (fvgb_residual(h, 0, res)) return report("fvgb_residual");
+        const bool print = istep == 1 || istep % rc.step_per_print == 0;
+        const bool write_hist = istep == 1 || istep % rc.step_per_output_hist == 0;
+        if (print && !quiet)
+            std::printf("step = %d\tt = %.9g\tresidual_rho = %.6e\tresidual_rhou = %.6e\tresidual_rhov = %.6e\t"
+                        "residual_rhoE = %.6e\n",
+                        istep, t, res[0], res[1], res[2], res[3]);
+        if (write_hist) {
+            std::fprintf(hist, "%d %.17g %.17g %.17g %.17g %.17g\n", istep, t, res[0], res[1], res[2], res[3]);
+            std::fflush(hist);
+        }
+        // modifySignalPack2_pause (CDriver.cpp:230-263)
+        if (std::isnan(res[0])) {
+            status = 2;
+            why = "NaN detected";
+            final_prefix = "nan_";
+            break;
+        }
+        if (t >= T) {
+            why = "physical time reached";
+            break;
+        }
+        if (res[0] <= kEpsilon) {
+            why = "steady state reached";
+            break;
+        }
+    }
+    std::fclose(hist);
+
+    if (fvgb_get_state(h, U.data())) return report("fvgb_get_state");
+    const std::string cont = out_dir + "/" + final_prefix + name + step_tag(istep) + ".dat";
+    if (fvgb_write_continue(mesh, cont.c_str(), t, istep, p.CFL, U.data())) return report(cont.c_str());
+    if (!quiet) std::printf("%s at step %d, t = %.17g; wrote %s\n", why, istep, t, cont.c_str());
+    fvgb_destroy(h);
+    fvgb_mesh_free(mesh);
+    return status;
+}

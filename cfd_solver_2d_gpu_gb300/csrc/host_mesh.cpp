@@ -116,6 +116,7 @@ int split(char* s, char** w, int maxw) {
 }  // namespace
 
 int read_su2(const char* path, int equation, double scale, HostMesh& m) {
+    RawMesh r;
     FILE* f = std::fopen(path, "rb");
     if (!f) return fail(FVGB_ERR_IO, std::string("cannot open mesh file ") + path);
     std::fseek(f, 0, SEEK_END);
@@ -126,12 +127,12 @@ int read_su2(const char* path, int equation, double scale, HostMesh& m) {
     std::fclose(f);
     buf[got] = 0;
 
-    std::vector<double> nx, ny;
-    std::vector<int> nid;
-    std::vector<int> tri;
-    struct Marker { std::string name; std::vector<int> e; };
-    std::vector<Marker> mk;
-    int maxnodeID = 1;
+    std::vector<double>& nx = r.nx;
+    std::vector<double>& ny = r.ny;
+    std::vector<int>& nid = r.nid;
+    std::vector<int>& tri = r.tri;
+    std::vector<RawMesh::Marker>& mk = r.mk;
+    int& maxnodeID = r.maxnodeID;
     enum { S_START, S_NDIME, S_NPOIN, S_NELEM, S_NMARK } state = S_START;
 
     char* p = buf.data();
@@ -172,7 +173,7 @@ int read_su2(const char* path, int equation, double scale, HostMesh& m) {
             if (!std::strcmp(w[0], "NMARK") || !std::strcmp(w[0], "MARKER_ELEMS")) {
             } else if (!std::strcmp(w[0], "MARKER_TAG")) {
                 if (nw < 3) return fail(FVGB_ERR_FORMAT, "malformed MARKER_TAG line");
-                mk.push_back(Marker{w[2], {}});
+                mk.push_back(RawMesh::Marker{w[2], {}});
             } else {
                 if (mk.empty() || nw < 3) return fail(FVGB_ERR_FORMAT, "boundary element before MARKER_TAG");
                 mk.back().e.push_back(std::atoi(w[1]) + 1);
@@ -191,6 +192,19 @@ int read_su2(const char* path, int equation, double scale, HostMesh& m) {
             }
         }
     }
+    return assemble(r, equation, m);
+}
+
+// FVM_2D::iniEdges .. iniEdges_lengths (FVMR/src/legacy/FVM_2D.cpp:36-198), the boundary
+// sets of SU2MeshReader.cpp:201-243 / ContinueFileReader::process (ContinueFileReader.cpp:457-494)
+// and OldDataConverter, in O(N): the reference's numbering and arrays.
+int assemble(RawMesh& r, int equation, HostMesh& m) {
+    std::vector<double>& nx = r.nx;
+    std::vector<double>& ny = r.ny;
+    std::vector<int>& nid = r.nid;
+    std::vector<int>& tri = r.tri;
+    std::vector<RawMesh::Marker>& mk = r.mk;
+    const int maxnodeID = r.maxnodeID;
     std::vector<int> idx((size_t)maxnodeID + 1, -1);
     for (size_t i = 0; i < nid.size(); i++)
         if (nid[i] >= 0) idx[nid[i]] = (int)i;
@@ -269,10 +283,12 @@ int read_su2(const char* path, int equation, double scale, HostMesh& m) {
         if (bt == -2) return fail(FVGB_ERR_MESH, "unknown boundary type " + mk[s].name);
         m.bc_type[s] = bt;
         m.bc_name[s] = mk[s].name;
-        size_t ne = mk[s].e.size() / 2;
+        size_t ne = r.marker_edge_ids ? mk[s].e.size() : mk[s].e.size() / 2;
         setedges[s].resize(ne);
         for (size_t k = 0; k < ne; k++) {
-            int ei = hm.get(mk[s].e[2 * k], mk[s].e[2 * k + 1]);
+            // edge IDs are 1-based positions in the assembled order (FVM_2D.cpp:121)
+            int ei = r.marker_edge_ids ? ((mk[s].e[k] >= 1 && mk[s].e[k] <= E) ? mk[s].e[k] - 1 : -1)
+                                       : hm.get(mk[s].e[2 * k], mk[s].e[2 * k + 1]);
             if (ei < 0) return fail(FVGB_ERR_MESH, "boundary edge is not an edge of the mesh");
             m.edge_set[ei] = s + 1;
             setedges[s][k] = ei;
@@ -302,6 +318,8 @@ int read_su2(const char* path, int equation, double scale, HostMesh& m) {
                 return fail(FVGB_ERR_MESH, "periodic boundary is not a translation of its pair");
         }
     }
+    m.node_id = nid;
+    m.set_edges = setedges;
     // OldDataConverter
     m.node_xy.resize(2 * (size_t)V);
     for (int i = 0; i < V; i++) {

@@ -347,3 +347,38 @@ extern "C" int fvgb_params_read_toml(const char* path, fvgb_params* p, char* mes
     if (!r.missing.empty()) return fail(FVGB_ERR_FORMAT, "input.toml: missing or mistyped keys:" + r.missing);
     return 0;
 }
+
+// The driver's keys of input.toml (TomlFileManager.cpp:110-148; defaults of
+// GlobalPara.cpp:26-29, 74-82): what CDriver::start reads besides the step's parameters.
+extern "C" int fvgb_run_config_read_toml(const char* path, fvgb_run_config* c) {
+    if (!path || !c) return fail(FVGB_ERR_ARG, "null argument");
+    Table t;
+    int rc = parse(path, t);
+    if (rc) return rc;
+    *c = fvgb_run_config{};
+    c->continue_run = 1;
+    c->step_per_print = 50;
+    c->step_per_output_field = 50;
+    c->step_per_output_hist = 50;
+    c->start_output_field = 0;
+    c->max_iteration = 5000;
+    c->tolerance_residual = 1.0e-7;
+    std::snprintf(c->filename, sizeof c->filename, "%s", "default_project");
+    std::snprintf(c->mesh_file_type, sizeof c->mesh_file_type, "%s", "inp");
+    Reader r{t, ""};
+    bool cont = true;
+    if (r.boolean("basic.continue", cont, false)) c->continue_run = cont ? 1 : 0;
+    std::string sv;
+    if (r.str("basic.filename", sv)) std::snprintf(c->filename, sizeof c->filename, "%s", sv.c_str());
+    if (r.str("basic.meshFileType", sv)) std::snprintf(c->mesh_file_type, sizeof c->mesh_file_type, "%s", sv.c_str());
+    r.integer("output.step_per_print", c->step_per_print, false);
+    r.integer("output.step_per_output_field", c->step_per_output_field, false);
+    r.integer("output.step_per_output_hist", c->step_per_output_hist, false);
+    r.integer("output.start_output_field", c->start_output_field, false);
+    r.integer("output.maxIteration", c->max_iteration, false);
+    r.num("output.tolerace_residual", c->tolerance_residual, false);
+    if (!r.missing.empty()) return fail(FVGB_ERR_FORMAT, "input.toml: wrong type for" + r.missing);
+    if (c->step_per_print <= 0 || c->step_per_output_field <= 0 || c->step_per_output_hist <= 0)
+        return fail(FVGB_ERR_FORMAT, "input.toml: output.step_per_* must be positive");
+    return 0;
+}

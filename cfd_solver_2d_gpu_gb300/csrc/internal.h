@@ -43,12 +43,32 @@ struct HostMesh {
     std::vector<double> edge_xy, edge_normal;               // 2E
     std::vector<int> bc_type;       // NB
     std::vector<std::string> bc_name;
+    std::vector<int> node_id;                  // V: the reference's node IDs (file index + 1)
+    std::vector<std::vector<int>> set_edges;   // NB: each boundary set's edges in set order
+    std::vector<double> U;                     // 4N: the state read with a continue file, else empty
+};
+
+// A mesh as read from a file, before assembly: node coordinates and IDs, triangles
+// as node IDs (quads already split), and the boundary markers, each a list of
+// node-ID pairs (.su2) or of 1-based edge IDs (continue file).
+struct RawMesh {
+    std::vector<double> nx, ny;
+    std::vector<int> nid;
+    std::vector<int> tri;
+    struct Marker {
+        std::string name;
+        std::vector<int> e;
+    };
+    std::vector<Marker> mk;
+    bool marker_edge_ids = false;
+    int maxnodeID = 1;
 };
 
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
 
 int read_su2(const char* path, int equation, double scale, HostMesh& m);
+int assemble(RawMesh& r, int equation, HostMesh& m);
 void mesh_view(const HostMesh& m, fvgb_mesh_soa& s);
 int initial_field(const fvgb_mesh_soa& s, const fvgb_params& p, double* U);
 

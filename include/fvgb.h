@@ -92,6 +92,21 @@ int fvgb_params_default(fvgb_params* p);
  * (FVMR/src/input/TomlFileManager.cpp:110-170, 200-265, mu0/Re 79-104).
  * mesh_name receives basic.filename (may be NULL). */
 int fvgb_params_read_toml(const char* path, fvgb_params* p, char* mesh_name, int mesh_name_len);
+/* What the driver loop reads from input.toml besides the step's parameters
+ * (CDriver::start, FVMR/src/drivers/CDriver.cpp:31-184; keys per
+ * TomlFileManager.cpp:110-148, defaults per GlobalPara.cpp:26-29, 74-82). */
+typedef struct fvgb_run_config {
+    int continue_run;            /* basic.continue: restart from the newest pause file */
+    int step_per_print;          /* output.step_per_print */
+    int step_per_output_field;   /* output.step_per_output_field */
+    int step_per_output_hist;    /* output.step_per_output_hist */
+    int start_output_field;      /* output.start_output_field */
+    int max_iteration;           /* output.maxIteration */
+    double tolerance_residual;   /* output.tolerace_residual (the reference's spelling) */
+    char filename[256];          /* basic.filename: mesh <filename>.su2, outputs <filename>... */
+    char mesh_file_type[16];     /* basic.meshFileType */
+} fvgb_run_config;
+int fvgb_run_config_read_toml(const char* path, fvgb_run_config* c);
 /* Reads and assembles an .su2 mesh with the reference's numbering
  * (SU2MeshReader::read_mesh_and_process, FVMR/src/input/SU2MeshReader.cpp:10-251,
  * FVM_2D::iniEdges.., FVMR/src/legacy/FVM_2D.cpp:36-198) in O(N). */
@@ -105,6 +120,24 @@ int fvgb_write_su2_periodic_square(const char* path, int n, double L, double jit
 int fvgb_write_su2_cylinder(const char* path, int n_theta, int n_r, double r0, double r1, double first_dr);
 /* Initial field (FieldInitializer, FVMR/src/input/FieldInitializer.cpp:129-222) on host. */
 int fvgb_initial_field(const fvgb_mesh_soa* mesh, const fvgb_params* p, double* U);
+
+/* Continue ("pause") files, the reference's restart format: t, istep, CFL, the
+ * nodes, the triangles with U and the boundary sets' edge IDs.  Written by
+ * FieldWriter::writeContinueFile_1 (FVMR/src/output/FieldWriter.cpp:264-326) and
+ * read by ContinueFileReader::readContinueFile_1 (FVMR/src/input/ContinueFileReader.cpp:
+ * 19-158, 457-494), which rebuilds the mesh from the file alone.  This writer
+ * uses 17 significant digits (the reference 6), so a restart continues bit for
+ * bit; the reference reads these files and this reader reads the reference's.
+ * fvgb_read_continue returns the mesh (its state through fvgb_continue_state),
+ * t, istep and the saved CFL (-1 when the file has none; the reference then
+ * keeps the input.toml value).  fvgb_write_continue takes a mesh from either
+ * reader and U[4][N] in reference numbering. */
+int fvgb_read_continue(const char* path, int equation, fvgb_mesh** out, double* t, int* istep, double* cfl);
+int fvgb_continue_state(const fvgb_mesh* m, double* U);
+int fvgb_write_continue(const fvgb_mesh* m, const char* path, double t, int istep, double cfl, const double* U);
+/* The newest pause_<name>[<n>].dat in directory, by the reference's rule
+ * (ContinueFileReader.cpp:24-53: largest n > 0); FVGB_ERR_IO when there is none. */
+int fvgb_find_continue_file(const char* directory, const char* name, char* path_out, int path_len);
 
 /* ---- one solver ----------------------------------------------------------- */
 

@@ -17,6 +17,9 @@
 //   ssprk3     Shu-Osher SSP-RK3 built the same way (new code 3104)
 //   rhs        one calculateFunctionF on the initial field, plus its dt
 //   mesh       assembly and initial field only
+//   continue   the newest pause_<basic.filename>[n].dat of the folder given in
+//              place of the mesh, read by ContinueFileReader::readContinueFile_1
+//              (FVMR/src/input/ContinueFileReader.cpp:19-158): mesh and field only
 // and writes every SoA array, the final field and the per-step dt to a small
 // binary file ("FVMRDUMP" + named arrays) that tests read with numpy.
 #include <cstdio>
@@ -29,6 +32,7 @@
 #include "input/TomlFileManager.h"
 #include "input/SU2MeshReader.h"
 #include "input/FieldInitializer.h"
+#include "input/ContinueFileReader.h"
 #include "solvers/GPUSolver2.h"
 #include "time/CIteration.h"
 #include "time/CalculateDt.h"
@@ -114,8 +118,18 @@ int main(int argc, char** argv) {
 
     TomlFileManager::getInstance()->readTomlFile(toml);
     GlobalPara::basic::useGPU = 0;
-    SU2MeshReader::read_mesh_and_process(mesh, true);
-    FieldInitializer::getInstance()->setInitialAndBoundaryCondition();
+    if (mode == "continue") {
+        // CInput::readField_1 with basic.continue: the newest pause_<basic.filename>[n].dat in
+        // the folder given in place of the mesh; the field initialiser is not called then
+        setenv("FVMR_REF_OUTDIR", mesh.c_str(), 1);
+        if (ContinueFileReader::readContinueFile_1() != 0) {
+            std::fprintf(stderr, "no continue file in %s\n", mesh.c_str());
+            return 5;
+        }
+    } else {
+        SU2MeshReader::read_mesh_and_process(mesh, true);
+        FieldInitializer::getInstance()->setInitialAndBoundaryCondition();
+    }
 
     GPU::GPUSolver2 s;
     s.allocateMemory();
@@ -154,7 +168,10 @@ int main(int argc, char** argv) {
         (double)GlobalPara::boundaryCondition::_2D::outlet::ruvp[0], (double)GlobalPara::boundaryCondition::_2D::outlet::ruvp[1],
         (double)GlobalPara::boundaryCondition::_2D::outlet::ruvp[2], (double)GlobalPara::boundaryCondition::_2D::outlet::ruvp[3]};
     d.f64("params", params);
-    if (mode == "mesh") return 0;
+    std::vector<double> cont = {(double)GlobalPara::time::t_previous, (double)GlobalPara::time::istep_previous,
+                                (double)GlobalPara::time::CFL};
+    d.f64("continue", cont);
+    if (mode == "mesh" || mode == "continue") return 0;
 
     std::vector<double> U0, R;
     copy_field(s.elementField_host.U, U0, N);

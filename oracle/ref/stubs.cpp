@@ -8,7 +8,13 @@
 #include <string>
 #include <new>
 
+#include <dirent.h>
+
+#include <algorithm>
+#include <vector>
+
 #include "output/LogWriter.h"
+#include "global/FilePathManager.h"
 #include "global/CExit.h"
 #include "output/FieldWriter.h"
 #include "drivers/RoutineController.h"
@@ -21,6 +27,27 @@
 #include "math/BasicAlgorithmGPU.h"
 
 static bool quiet() { return std::getenv("FVMR_REF_VERBOSE") == nullptr; }
+
+// The harness's continue mode: ContinueFileReader looks for pause files in the
+// output folder, which here is the folder named by FVMR_REF_OUTDIR.
+FilePathManager* FilePathManager::getInstance() {
+    static FilePathManager* p = new FilePathManager();
+    return p;
+}
+void FilePathManager::initialzeVariables() {
+    const char* d = std::getenv("FVMR_REF_OUTDIR");
+    m_outputDirectory = std::string(d ? d : ".") + "/";
+}
+std::vector<std::string> FilePathManager::getFiles(std::string path) {
+    std::vector<std::string> out;
+    if (DIR* d = opendir(path.c_str())) {
+        while (dirent* e = readdir(d))
+            if (e->d_name[0] != '.') out.push_back(e->d_name);
+        closedir(d);
+    }
+    std::sort(out.begin(), out.end());
+    return out;
+}
 
 void LogWriter::log(std::string, LogLevel) {}
 void LogWriter::print(std::string c, LogLevel) { if (!quiet()) std::fputs(c.c_str(), stderr); }

@@ -68,6 +68,46 @@ def golden_cases(d):
     ]
 
 
+CONTINUE_DIR = os.path.join(HERE, "continue")
+REF_MESH_KEYS = MESH_KEYS + ["edge_dist"]
+
+
+def continue_cases(d):
+    """(name, toml text, su2 path, equation) of the continue-file fixtures."""
+    T = cases.toml_text
+    return [
+        ("jsquare12", T(equation=1, filename="jsquare12"), cases.square_mesh(12, jitter=0.2, directory=d), 1),
+        ("cylinder16_ns", T(equation=2, filename="cylinder16_ns", ic_type=1, inf_mode=0, Ma=0.2, Re=100.0),
+         cases.cylinder_mesh(16, 8, directory=d), 2),
+    ]
+
+
+def make_continue(d):
+    """Continue files written by this library (fvgb_write_continue, seeded state) and the
+    arrays the reference's ContinueFileReader builds from them (oracle/_ref, continue mode)."""
+    import cfd_solver_2d_gpu_gb300 as fv
+    os.makedirs(CONTINUE_DIR, exist_ok=True)
+    for name, toml, su2, eq in continue_cases(d):
+        m = fv.Mesh.read_su2(su2, equation=eq)
+        U = np.random.default_rng(20261203).uniform(0.5, 2.0, (4, m.N))
+        folder = os.path.join(d, "cont_" + name)
+        os.makedirs(folder, exist_ok=True)
+        path = os.path.join(folder, f"pause_{name}[0042].dat")
+        m.write_continue(path, U, 0.123456789012345678, 42, 0.8)
+        tp = os.path.join(folder, "input.toml")
+        with open(tp, "w") as f:
+            f.write(toml)
+        ref = run_ref(REF, tp, folder, "continue", 0, os.path.join(d, name + "_cont.bin"))
+        out = {k: ref[k] for k in REF_MESH_KEYS}
+        out.update(continue_info=ref["continue"],
+                   toml=np.frombuffer(toml.encode(), dtype=np.uint8),
+                   pause_gz=np.frombuffer(gzip.compress(open(path, "rb").read(), mtime=0), dtype=np.uint8),
+                   equation=np.array([eq]))
+        dst = os.path.join(CONTINUE_DIR, name + ".npz")
+        np.savez_compressed(dst, **out)
+        print(f"{dst}: N={ref['sizes'][0]} ({os.path.getsize(dst) // 1024} KiB)")
+
+
 def run_ref(binary, toml_path, su2, mode, steps, out):
     r = subprocess.run([binary, toml_path, su2, mode, str(steps), out], capture_output=True, text=True)
     if r.returncode != 0:
@@ -97,6 +137,7 @@ def main():
             path = os.path.join(HERE, name + ".npz")
             np.savez_compressed(path, **out)
             print(f"{path}: N={rhs['sizes'][0]} {mode} x{steps} ({os.path.getsize(path) // 1024} KiB)")
+        make_continue(d)
 
 
 def load(name):

@@ -1,0 +1,81 @@
+"""The headless driver (fvgb_run, csrc/driver/fvgb_run.cpp) on the GPU: its loop
+gives the same state as stepping through the C ABI directly, a run stopped and
+restarted from its pause file ends bit for bit where an unbroken run ends, and a
+NaN ends the run with status 2 and a nan_ continue file (as CDriver::start's
+signal packs, FVMR/src/drivers/CDriver.cpp:202-263)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import cfd_solver_2d_gpu_gb300 as fv
+from cfd_solver_2d_gpu_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+EXE = os.path.join(os.path.dirname(fv.__file__), "fvgb_run")
+
+
+def make_case(d, max_iteration, cont=False):
+    os.makedirs(d, exist_ok=True)
+    text = cases.toml_text(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.8,
+                           filename="jv", max_iteration=max_iteration)
+    text = text.replace("step_per_print = 50", "step_per_print = 10").replace(
+        "step_per_output_hist = 100", "step_per_output_hist = 5")
+    if cont:
+        text = text.replace("continue = false", "continue = true")
+    tp = os.path.join(d, "input.toml")
+    with open(tp, "w") as f:
+        f.write(text)
+    shutil.copy(cases.square_mesh(24, jitter=0.2), os.path.join(d, "jv.su2"))
+    return tp
+
+
+def run(tp, out):
+    fv.lib()
+    return subprocess.run([EXE, tp, "--output", out], capture_output=True, text=True)
+
+
+def test_driver_matches_direct_stepping(tmp_path):
+    d = str(tmp_path / "case")
+    tp = make_case(d, 30)
+    r = run(tp, os.path.join(d, "out"))
+    assert r.returncode == 0, r.stderr
+    mesh, U, t, istep, cfl = fv.Mesh.read_continue(os.path.join(d, "out", "pause_jv[0030].dat"))
+    assert istep == 30 and cfl == 0.8
+    p = fv.Params.from_toml(tp)
+    m = fv.Mesh.read_su2(os.path.join(d, "jv.su2"), p)
+    s = fv.GPUSolver2(m, p)
+    t2 = s.step(0.0, p.T_end, 30)
+    assert np.array_equal(s.get_state(), U) and t2 == t
+    hist = open(os.path.join(d, "out", "jv_hist.dat")).read().split("\n")
+    assert hist[0].startswith("VARIABLES") and [int(l.split()[0]) for l in hist[1:] if l] == [1, 5, 10, 15, 20,
+                                                                                           25, 30]
+    assert "step = 10" in r.stdout and "step = 30" in r.stdout
+
+
+def test_restart_continues_bit_for_bit(tmp_path):
+    one = str(tmp_path / "one")
+    assert run(make_case(one, 30), os.path.join(one, "out")).returncode == 0
+    two = str(tmp_path / "two")
+    out = os.path.join(two, "out")
+    assert run(make_case(two, 12), out).returncode == 0
+    r = run(make_case(two, 30, cont=True), out)  # basic.continue: resumes from pause_jv[0012].dat
+    assert r.returncode == 0 and "continue from" in r.stdout, r.stdout + r.stderr
+    _, Ua, ta, ia, _ = fv.Mesh.read_continue(os.path.join(one, "out", "pause_jv[0030].dat"))
+    _, Ub, tb, ib, _ = fv.Mesh.read_continue(os.path.join(out, "pause_jv[0030].dat"))
+    assert ia == ib == 30 and ta == tb and np.array_equal(Ua, Ub)
+
+
+def test_nan_stops_with_status_2(tmp_path):
+    d = str(tmp_path / "nan")
+    out = os.path.join(d, "out")
+    assert run(make_case(d, 3), out).returncode == 0
+    mesh, U, t, istep, cfl = fv.Mesh.read_continue(os.path.join(out, "pause_jv[0003].dat"))
+    U[:, 17] = np.nan
+    os.remove(os.path.join(out, "pause_jv[0003].dat"))
+    mesh.write_continue(os.path.join(out, "pause_jv[0004].dat"), U, t, 4, cfl)
+    r = run(make_case(d, 20, cont=True), out)
+    assert r.returncode == 2, (r.returncode, r.stdout, r.stderr)
+    assert any(f.startswith("nan_jv[") for f in os.listdir(out))
