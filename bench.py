@@ -209,6 +209,23 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(x, world):
+    """The largest x over the ranks: a replicated job takes as long as its slowest rank."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(cells, stages, steps, world, seconds):
+    """Whole-job cell-stage updates/s of world replicas, each advancing cells x stages x steps."""
+    return stages * cells * steps * world / seconds
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -415,12 +432,9 @@ def main():
             ms = s.step_timed(T, args.steps)
         barrier()
         launches = s.kernel_launches() - l0
-        if world > 1:
-            tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            ms = float(tt.item())
+        ms = max_over_ranks(ms, world)
         clocks = clk.summary()
-        value = 3.0 * N * args.steps * world / (ms / 1e3)
+        value = job_throughput(N, 3, args.steps, world, ms / 1e3)
 
         # per-kernel-group device times (same steps, launched one by one with events)
         prof = s.profile_steps(T, max(3, min(args.steps, 20)))
@@ -464,8 +478,8 @@ def main():
                 t = s.step(t, T, 1)
                 s.get_state_ptr(host.data_ptr())
             barrier()
-            el = time.perf_counter() - t0
-            e2e = {"value": 3.0 * N * k_e2e * world / el, "unit": "cell-stage updates/s",
+            el = max_over_ranks(time.perf_counter() - t0, world)
+            e2e = {"value": job_throughput(N, 3, k_e2e, world, el), "unit": "cell-stage updates/s",
                    "h2d_bytes_per_step": 32 * N, "d2h_bytes_per_step": 32 * N, "steps": k_e2e,
                    "api": "fvgb_set_state + fvgb_step + fvgb_get_state (pinned host buffers)"}
 

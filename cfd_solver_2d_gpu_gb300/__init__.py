@@ -38,7 +38,7 @@ class Params(ctypes.Structure):
         (n, ctypes.c_double) for n in ("gamma", "R", "Pr", "mu0", "T0", "CFL", "T_end", "Re")] + [
         ("inf", ctypes.c_double * 4), ("inlet", ctypes.c_double * 4), ("outlet", ctypes.c_double * 4),
         ("vortex", ctypes.c_double * 3), ("shock", ctypes.c_double * 4), ("mesh_scale", ctypes.c_double),
-        ("max_iteration", ctypes.c_int), ("pad_", ctypes.c_int)]
+        ("max_iteration", ctypes.c_int), ("pad_", ctypes.c_int), ("ref_area", ctypes.c_double)]
 
     @classmethod
     def default(cls):
@@ -61,7 +61,8 @@ class MeshSoA(ctypes.Structure):
         (n, ctypes.c_void_p) for n in ("node_xy", "elem_nodes", "elem_edges", "elem_neighbors", "elem_xy",
                                        "elem_volume", "edge_nodes", "edge_L", "edge_R", "edge_setID",
                                        "edge_periodicPair", "edge_length", "edge_distance", "edge_xy",
-                                       "edge_normal", "boundary_type")]
+                                       "edge_normal", "boundary_type", "set_edge_offsets", "set_edge_list",
+                                       "set_names")]
 
 
 _lib = None
@@ -123,6 +124,13 @@ def lib():
             "fvgb_batch_tune": (i, [v, i, c, i]),
             "fvgb_batch_info": (i, [v, ctypes.POINTER(ctypes.c_longlong)]),
             "fvgb_fp64_peak": (i, [i, dp]),
+            "fvgb_node_field": (i, [v, dp]),
+            "fvgb_boundary_forces": (i, [v, dp, dp, dp, dp]),
+            "fvgb_write_tecplot_volume": (i, [v, c, c, d, i]),
+            "fvgb_write_tecplot_boundary": (i, [v, c, d, i]),
+            "fvgb_colour_nodes": (i, [v, d, d, ctypes.POINTER(ctypes.POINTER(ctypes.c_float)),
+                                      ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+            "fvgb_num_nodes": (i, [v, ip]),
             "fvgb_last_error": (c, []),
             "fvgb_version": (c, []),
         }
@@ -198,7 +206,9 @@ class Mesh:
                 "edge_nodes": ("i", (2, E)), "edge_L": ("i", (E,)), "edge_R": ("i", (E,)),
                 "edge_setID": ("i", (E,)), "edge_periodicPair": ("i", (E,)), "edge_length": ("d", (E,)),
                 "edge_distance": ("d", (E,)), "edge_xy": ("d", (2, E)), "edge_normal": ("d", (2, E)),
-                "boundary_type": ("i", (NB,))}
+                "boundary_type": ("i", (NB,)), "set_edge_offsets": ("i", (NB + 1,))}
+        if name == "set_edge_list":
+            spec[name] = ("i", (int(self.array("set_edge_offsets")[-1]),))
         code, shape = spec[name]
         ct = ctypes.c_double if code == "d" else ctypes.c_int
         n = int(np.prod(shape))
@@ -212,7 +222,8 @@ class RunConfig(ctypes.Structure):
                 ("step_per_output_field", ctypes.c_int), ("step_per_output_hist", ctypes.c_int),
                 ("start_output_field", ctypes.c_int), ("max_iteration", ctypes.c_int),
                 ("tolerance_residual", ctypes.c_double), ("filename", ctypes.c_char * 256),
-                ("mesh_file_type", ctypes.c_char * 16)]
+                ("mesh_file_type", ctypes.c_char * 16), ("volume_preset", ctypes.c_int),
+                ("boundary_preset", ctypes.c_int)]
 
 
 def run_config(path):
@@ -329,6 +340,43 @@ class GPUSolver2:
         out = ctypes.c_double()
         _check(lib().fvgb_dt(self._h, ctypes.byref(out)))
         return out.value
+
+    # field output --------------------------------------------------------------
+    def node_field(self):
+        """FieldWriter::update_nodeField on the device: (6, V) = rho, u, v, p, Cp, Ma per node."""
+        out = np.empty((6, self.num_nodes()))
+        _check(lib().fvgb_node_field(self._h, _dp(out)))
+        return out
+
+    def num_nodes(self):
+        v = ctypes.c_int()
+        _check(lib().fvgb_num_nodes(self._h, ctypes.byref(v)))
+        return v.value
+
+    def boundary_forces(self, n_sets):
+        """calculate_edgeSet_force: (CD[NB], CL[NB], CD_wall, CL_wall)."""
+        cd, cl = np.empty(n_sets), np.empty(n_sets)
+        dw, lw = ctypes.c_double(), ctypes.c_double()
+        _check(lib().fvgb_boundary_forces(self._h, _dp(cd), _dp(cl), ctypes.byref(dw), ctypes.byref(lw)))
+        return cd, cl, dw.value, lw.value
+
+    def write_tecplot_volume(self, path, t, title="title", preset=2):
+        _check(lib().fvgb_write_tecplot_volume(self._h, os.fsencode(path), title.encode(), float(t), int(preset)))
+
+    def write_tecplot_boundary(self, path, t, preset=1):
+        _check(lib().fvgb_write_tecplot_boundary(self._h, os.fsencode(path), float(t), int(preset)))
+
+    def colour_nodes(self, range_lo=0.0, range_hi=1.0):
+        """The GUI's field colouring into a device buffer; returns (rgb (V, 3) float32, node values (V,),
+        device pointer of the [V][3] buffer)."""
+        V = self.num_nodes()
+        rgb = np.empty((V, 3), dtype=np.float32)
+        val = np.empty(V, dtype=np.float32)
+        dev = ctypes.POINTER(ctypes.c_float)()
+        fp = ctypes.POINTER(ctypes.c_float)
+        _check(lib().fvgb_colour_nodes(self._h, float(range_lo), float(range_hi), ctypes.byref(dev),
+                                       rgb.ctypes.data_as(fp), val.ctypes.data_as(fp)))
+        return rgb, val, ctypes.cast(dev, ctypes.c_void_p).value
 
     def update_residual_vector(self, norm=0):
         out = np.zeros(4)

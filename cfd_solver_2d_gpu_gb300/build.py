@@ -43,7 +43,8 @@ def build(verbose=False, force=False):
     if not force and not _stale(LIB, srcs + headers + [__file__]):
         build_driver(force)
         return LIB
-    common = [nvcc(), "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
+    # -ffp-contract=off: host arithmetic (layout coefficients, forces) rounds the same on x86 and Arm
+    common = [nvcc(), "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "-I", os.path.join(ROOT, "include"), "-I", CSRC] + ARCH
     if os.environ.get("FVGB_PTXAS_VERBOSE"):
         common += ["-Xptxas", "-v"]

@@ -10,8 +10,14 @@
 // initial field.  The loop follows CDriver::start and its signal packs
 // (CDriver.cpp:202-263):
 //   - print the residual at step 1 and every output.step_per_print steps;
-//   - append a line to <filename>_hist.dat at step 1 and every
-//     output.step_per_output_hist steps;
+//   - append a line (iteration, t, the four residuals, C_L and C_D of the
+//     walls) to <filename>_hist.dat at step 1 and every
+//     output.step_per_output_hist steps (FieldWriter::write_tecplot_hist_file,
+//     FVMR/src/output/FieldWriter.cpp:211-262);
+//   - write the Tecplot volume file <filename>[istep].dat and the boundary file
+//     <filename>_tec_boundary.dat at step 1, every output.step_per_output_field
+//     steps from output.start_output_field on, and at the stop
+//     (FieldWriter.cpp:44-172, presets output.outputScheme_*_preset);
 //   - stop at output.maxIteration, when the residual of rho falls to 1e-10
 //     (U2NITS::Math::EPSILON), when the time reaches max_physical_time, or on
 //     NaN; write pause_<filename>[istep].dat (istep as %04d) at the stop, or
@@ -22,7 +28,8 @@
 //     stepping with dt = 0 until maxIteration. This driver stops at the first
 //     output event at which t has reached T.
 //   - Continue files carry 17 significant digits (the reference's 6).
-//   - The hist file holds iteration, t and the four residuals.
+//   - Node values in the Tecplot files come from the state after the step; the
+//     reference's come from the primitive variables of the step's start.
 // Exit status: 0 at a normal stop, 2 after NaN or an out-of-range state,
 // 1 on any other error.
 #include <sys/stat.h>
@@ -125,14 +132,27 @@ int main(int argc, char** argv) {
     if (fvgb_create(&soa, &p, &h)) return report("fvgb_create");
     if (fvgb_set_state(h, U.data())) return report("fvgb_set_state");
 
+    // write_tecplot_hist_file: the head when the file is new or the run did not restart
     const std::string hist_path = out_dir + "/" + name + "_hist.dat";
-    FILE* hist = std::fopen(hist_path.c_str(), restarted ? "a" : "w");
+    bool hist_head = !restarted;
+    if (FILE* probe = std::fopen(hist_path.c_str(), "r")) std::fclose(probe);
+    else hist_head = true;
+    FILE* hist = std::fopen(hist_path.c_str(), hist_head ? "w" : "a");
     if (!hist) {
         std::fprintf(stderr, "fvgb_run: cannot write %s\n", hist_path.c_str());
         return 1;
     }
-    if (!restarted) std::fprintf(hist, "VARIABLES = \"Iteration\" \"Time\" \"Residual_rho\" \"Residual_rhou\" "
-                                       "\"Residual_rhov\" \"Residual_rhoE\"\n");
+    if (hist_head)
+        std::fprintf(hist, "title= \"tecplot hist file\"\nvariables= \"Iteration\", \"physical_time\", \"R_1\", "
+                           "\"R_2\", \"R_3\", \"R_4\", \"C_L\", \"C_D\"\nzone t= \"zone title\", f= point\n");
+    std::vector<double> cd_set(soa.num_boundary > 0 ? soa.num_boundary : 1), cl_set(cd_set.size());
+    auto write_fields = [&](int at) -> int {
+        const std::string vol = out_dir + "/" + name + step_tag(at) + ".dat";
+        const std::string bnd = out_dir + "/" + name + "_tec_boundary.dat";
+        if (fvgb_write_tecplot_volume(h, vol.c_str(), "title", t, rc.volume_preset)) return report(vol.c_str());
+        if (fvgb_write_tecplot_boundary(h, bnd.c_str(), t, rc.boundary_preset)) return report(bnd.c_str());
+        return 0;
+    };
 
     const double T = p.T_end;
     const int max_it = rc.max_iteration;
@@ -141,12 +161,14 @@ int main(int argc, char** argv) {
     const char* why = "maximum iteration reached";
     std::string final_prefix = "pause_";
     auto next_multiple = [](int after, int every) { return (after / every + 1) * every; };
+    int last_field_step = -1;
     while (istep < max_it) {
         // the next step at which CDriver::start would print or write (modifySignalPack1_output)
         int target = max_it;
         if (istep == 0) target = 1;
         target = std::min(target, next_multiple(istep, rc.step_per_print));
         target = std::min(target, next_multiple(istep, rc.step_per_output_hist));
+        target = std::min(target, next_multiple(istep, rc.step_per_output_field));
         int rcs = fvgb_step(h, &t, T, target - istep);
         if (rcs == FVGB_ERR_NAN || rcs == FVGB_ERR_RANGE) {
             std::fprintf(stderr, "fvgb_run: %s near step %d\n", fvgb_last_error(), target);
@@ -162,13 +184,21 @@ int main(int argc, char** argv) {
         if (fvgb_residual(h, 0, res)) return report("fvgb_residual");
         const bool print = istep == 1 || istep % rc.step_per_print == 0;
         const bool write_hist = istep == 1 || istep % rc.step_per_output_hist == 0;
+        const bool write_field =
+            istep == 1 || (istep % rc.step_per_output_field == 0 && istep >= rc.start_output_field);
         if (print && !quiet)
             std::printf("step = %d\tt = %.9g\tresidual_rho = %.6e\tresidual_rhou = %.6e\tresidual_rhov = %.6e\t"
                         "residual_rhoE = %.6e\n",
                         istep, t, res[0], res[1], res[2], res[3]);
         if (write_hist) {
-            std::fprintf(hist, "%d %.17g %.17g %.17g %.17g %.17g\n", istep, t, res[0], res[1], res[2], res[3]);
+            double cdw = 0.0, clw = 0.0;
+            if (fvgb_boundary_forces(h, cd_set.data(), cl_set.data(), &cdw, &clw)) return report("forces");
+            std::fprintf(hist, "%d %e %e %e %e %e %e %e\n", istep, t, res[0], res[1], res[2], res[3], clw, cdw);
             std::fflush(hist);
+        }
+        if (write_field) {
+            if (write_fields(istep)) return 1;
+            last_field_step = istep;
         }
         // modifySignalPack2_pause (CDriver.cpp:230-263)
         if (std::isnan(res[0])) {
@@ -187,6 +217,8 @@ int main(int argc, char** argv) {
         }
     }
     std::fclose(hist);
+    // every stop writes the field too (modifySignalPack2_pause sets b_writeTecplot)
+    if (last_field_step != istep && write_fields(istep)) return 1;
 
     if (fvgb_get_state(h, U.data())) return report("fvgb_get_state");
     const std::string cont = out_dir + "/" + final_prefix + name + step_tag(istep) + ".dat";

@@ -420,6 +420,18 @@ void mesh_view(const HostMesh& m, fvgb_mesh_soa& s) {
     s.edge_xy = m.edge_xy.data();
     s.edge_normal = m.edge_normal.data();
     s.boundary_type = m.bc_type.data();
+    m.set_off.assign(1, 0);
+    m.set_list.clear();
+    m.name_ptrs.clear();
+    for (int b = 0; b < m.NB; b++) {
+        if (b < (int)m.set_edges.size()) m.set_list.insert(m.set_list.end(), m.set_edges[b].begin(), m.set_edges[b].end());
+        m.set_off.push_back((int)m.set_list.size());
+        m.name_ptrs.push_back(b < (int)m.bc_name.size() ? m.bc_name[b].c_str() : "");
+    }
+    const bool have_sets = (int)m.set_edges.size() == m.NB;
+    s.set_edge_offsets = have_sets ? m.set_off.data() : nullptr;
+    s.set_edge_list = have_sets ? m.set_list.data() : nullptr;
+    s.set_names = m.name_ptrs.data();
 }
 
 // ruvp2U_host, FVMR/src/math/PhysicalKernel.h:20-27

@@ -247,6 +247,7 @@ extern "C" int fvgb_params_default(fvgb_params* p) {
     p->vortex[2] = 1;
     p->mesh_scale = 1.0;
     p->max_iteration = 5000;
+    p->ref_area = 1.0;
     return 0;
 }
 
@@ -266,6 +267,7 @@ extern "C" int fvgb_params_read_toml(const char* path, fvgb_params* p, char* mes
     r.num("constant.mesh_scale_factor", scale, false);
     p->mesh_scale = scale;
     refA *= scale;
+    p->ref_area = refA;
     // boundary states (T0 and gamma already read, p0 of the config is used for Ma input)
     {
         fvgb_params tmp = *p;
@@ -363,6 +365,8 @@ extern "C" int fvgb_run_config_read_toml(const char* path, fvgb_run_config* c) {
     c->start_output_field = 0;
     c->max_iteration = 5000;
     c->tolerance_residual = 1.0e-7;
+    c->volume_preset = 2;    // FieldWriter.h:92-93: type_ruvp_Ma, type_ruvp_Cp
+    c->boundary_preset = 1;
     std::snprintf(c->filename, sizeof c->filename, "%s", "default_project");
     std::snprintf(c->mesh_file_type, sizeof c->mesh_file_type, "%s", "inp");
     Reader r{t, ""};
@@ -377,6 +381,10 @@ extern "C" int fvgb_run_config_read_toml(const char* path, fvgb_run_config* c) {
     r.integer("output.start_output_field", c->start_output_field, false);
     r.integer("output.maxIteration", c->max_iteration, false);
     r.num("output.tolerace_residual", c->tolerance_residual, false);
+    r.integer("output.outputScheme_volume_preset", c->volume_preset, false);
+    r.integer("output.outputScheme_boundary_preset", c->boundary_preset, false);
+    if (c->volume_preset < 0 || c->volume_preset > 2 || c->boundary_preset < 0 || c->boundary_preset > 2)
+        return fail(FVGB_ERR_FORMAT, "input.toml: output scheme presets are 0, 1 or 2");
     if (!r.missing.empty()) return fail(FVGB_ERR_FORMAT, "input.toml: wrong type for" + r.missing);
     if (c->step_per_print <= 0 || c->step_per_output_field <= 0 || c->step_per_output_hist <= 0)
         return fail(FVGB_ERR_FORMAT, "input.toml: output.step_per_* must be positive");

@@ -46,6 +46,9 @@ struct HostMesh {
     std::vector<int> node_id;                  // V: the reference's node IDs (file index + 1)
     std::vector<std::vector<int>> set_edges;   // NB: each boundary set's edges in set order
     std::vector<double> U;                     // 4N: the state read with a continue file, else empty
+    // flattened set_edges and the names' C strings, filled by mesh_view for fvgb_mesh_soa
+    mutable std::vector<int> set_off, set_list;
+    mutable std::vector<const char*> name_ptrs;
 };
 
 // A mesh as read from a file, before assembly: node coordinates and IDs, triangles

@@ -112,6 +112,7 @@ int Solver::init(const fvgb_mesh_soa& m, const fvgb_params& prm) {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     rc = build_layout(m, p, L);
     if (rc) return rc;
+    if ((rc = keep_output_mesh(m))) return rc;
     N = L.N;
     E = L.E;
     gas = make_gas(p);
@@ -190,6 +191,7 @@ int Solver::init(const fvgb_mesh_soa& m, const fvgb_params& prm) {
 }
 
 Solver::~Solver() {
+    release_output();
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (h_state) cudaFreeHost(h_state);
     for (void* q : owned) cudaFree(q);

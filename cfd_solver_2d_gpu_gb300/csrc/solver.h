@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <string>
 #include <vector>
 
 #include "internal.h"
@@ -47,6 +48,22 @@ struct Solver {
     dev::StepState* d_state = nullptr;
     dev::StepState* h_state = nullptr;
     dev::Status* d_status = nullptr;
+
+    // what the output functions need (output.cu), in reference numbering: node
+    // coordinates, the cells' nodes, and per boundary set its edges in set order
+    struct OutputMesh {
+        int V = 0, NB = 0;
+        std::vector<double> node_xy;                 // 2V
+        std::vector<int> elem_nodes;                 // 3N
+        std::vector<int> set_off;                    // NB+1
+        std::vector<int> set_n0, set_n1;             // per set edge: its two nodes
+        std::vector<double> set_nx, set_ny, set_len;  // per set edge: normal and length
+        std::vector<int> set_type;
+        std::vector<std::string> set_name;
+    } om;
+    struct OutputState* out = nullptr;  // device node lists and buffers, made on first use
+    int keep_output_mesh(const fvgb_mesh_soa& m);
+    void release_output();
 
     // kernel groups timed by profile_steps()
     enum { PROF_DT = 0, PROF_GRAD = 1, PROF_FLUX = 2, PROF_UPDATE = 3, PROF_RESTRICT = 4, PROF_NCLASS = 5 };

@@ -55,6 +55,7 @@ typedef struct fvgb_params {
     double mesh_scale;   /* constant.mesh_scale_factor */
     int max_iteration;   /* output.maxIteration */
     int pad_;
+    double ref_area;     /* constant.referenceArea x mesh_scale_factor (TomlFileManager.cpp:128-131) */
 } fvgb_params;
 
 /* Reference-order mesh arrays, mirroring GPU::NodeSoA / ElementSoA / EdgeSoA /
@@ -78,6 +79,13 @@ typedef struct fvgb_mesh_soa {
     const double* edge_xy;        /* [2][E] */
     const double* edge_normal;    /* [2][E] */
     const int* boundary_type;     /* [NB] */
+    /* each boundary set's edges in set order (VirtualBoundarySet_2D::pEdges, the
+     * BoundaryV2 edge sets of OldDataConverter.cpp:179-193): set s holds
+     * set_edge_list[set_edge_offsets[s] .. set_edge_offsets[s+1]); may be NULL, then
+     * the edges of a set are taken in edge order */
+    const int* set_edge_offsets;  /* [NB+1] */
+    const int* set_edge_list;
+    const char* const* set_names; /* [NB] marker names, may be NULL */
 } fvgb_mesh_soa;
 
 typedef struct fvgb_mesh fvgb_mesh;     /* host mesh owned by the library */
@@ -105,6 +113,8 @@ typedef struct fvgb_run_config {
     double tolerance_residual;   /* output.tolerace_residual (the reference's spelling) */
     char filename[256];          /* basic.filename: mesh <filename>.su2, outputs <filename>... */
     char mesh_file_type[16];     /* basic.meshFileType */
+    int volume_preset;           /* output.outputScheme_volume_preset: 0 rho u v p, 1 + Cp, 2 + Ma (default 2) */
+    int boundary_preset;         /* output.outputScheme_boundary_preset (default 1) */
 } fvgb_run_config;
 int fvgb_run_config_read_toml(const char* path, fvgb_run_config* c);
 /* Reads and assembles an .su2 mesh with the reference's numbering
@@ -190,6 +200,37 @@ int fvgb_step_timed(fvgb_handle* h, double T, int nsteps, double* ms_out);
  * [4] positivity pass.  (The reference times only whole iterations with
  * std::chrono, FVMR/src/drivers/CDriver.cpp:73-85.) */
 int fvgb_profile_steps(fvgb_handle* h, double T, int nsteps, double ms_out[5], int count_out[5]);
+
+/* ---- field output ----------------------------------------------------------
+ * Node values of the current state, as FieldWriter::update_nodeField
+ * (FVMR/src/output/FieldWriter.cpp:364-453) forms them for its Tecplot files:
+ * per node the mean of its cells' rho, u, v, p (summed in cell order), then
+ * Cp = (p - p_inf) / (1/2 rho_inf V_inf^2) and Ma.  out6[6][V] = rho, u, v, p,
+ * Cp, Ma in reference node numbering (may be NULL).  Computed on the device. */
+int fvgb_node_field(fvgb_handle* h, double* out6);
+/* Pressure lift and drag coefficients per boundary set (ReferenceData::
+ * calculate_edgeSet_force, FieldWriter.cpp:175-210: Cp of the edge's nodes
+ * averaged, times length / referenceArea, along the edge normal) and their sums
+ * over the wall sets (HistData::set_CDCL_wall, FieldWriter.cpp:611-632).  cd/cl
+ * are [NB] (either may be NULL). */
+int fvgb_boundary_forces(fvgb_handle* h, double* cd, double* cl, double* cd_wall, double* cl_wall);
+/* Tecplot ASCII files of write_tecplot_volume_file / write_tecplot_boundary_file
+ * (FieldWriter.cpp:44-172): preset 0 = x y rho u v p, 1 = + Cp, 2 = + Ma
+ * (output.outputScheme_*_preset; the reference's defaults are 2 for the volume
+ * and 1 for the boundary file). */
+int fvgb_write_tecplot_volume(fvgb_handle* h, const char* path, const char* title, double t, int preset);
+int fvgb_write_tecplot_boundary(fvgb_handle* h, const char* path, double t, int preset);
+/* The field colouring of the reference's GUI (FVMR/src/gui/cuda/CudaGrid_kernels.cu:
+ * 18-164, 225-245) without a graphics stack: per node the largest density of its
+ * cells (the reference's racy max of rho x count, times 1/count, done here
+ * deterministically), normalised by [range_lo, range_hi] (render.range_1/2)
+ * and mapped through the reference's five-point colour map.  The colours
+ * go to a device buffer owned by the handle, [V][3] floats (*rgb_dev, valid
+ * until the next call or fvgb_destroy); rgb_host [V][3] and node_value_host [V]
+ * receive copies when not NULL. */
+int fvgb_colour_nodes(fvgb_handle* h, double range_lo, double range_hi, float** rgb_dev, float* rgb_host,
+                      float* node_value_host);
+int fvgb_num_nodes(fvgb_handle* h, int* V);
 
 /* ---- discrete adjoint ------------------------------------------------------
  * No counterpart in the reference.  Reverse-mode derivative of K steps of the

@@ -1157,3 +1157,118 @@ void om_residual(const om_mesh* m, const double* rhs, int norm, double* out) {
         out[v] = s;
     }
 }
+
+/* ---- field output ------------------------------------------------------- */
+
+/* FieldWriter::update_nodeField_ruvp (FVMR/src/output/FieldWriter.cpp:370-402) over
+ * CIteration::update_host_ruvp_Uold's U2ruvp (FVMR/src/time/CIteration.cpp:163-180),
+ * then update_nodeField_other_variables (FieldWriter.cpp:404-430) and
+ * ReferenceData::update_farfield (FieldWriter.cpp:540-549) for p_inf, pdyn_inf */
+void om_node_field(int N, int V, const int* elem_nodes, const double* U, double gamma, double p_inf,
+                   double pdyn_inf, double* out) {
+    int* cnt = (int*)calloc((size_t)(V > 0 ? V : 1), sizeof(int));
+    for (int k = 0; k < 4; k++) memset(out + (size_t)k * V, 0, sizeof(double) * (size_t)V);
+    for (int e = 0; e < N; e++) {
+        const double r = U[e], uu = U[(size_t)N + e] / U[e], vv = U[2 * (size_t)N + e] / U[e];
+        const double pp = r * (gamma - 1) * (U[3 * (size_t)N + e] / U[e] - (uu * uu + vv * vv) * 0.5);
+        const double ruvp[4] = {r, uu, vv, pp};
+        for (int j = 0; j < 4; j++) {
+            const int n = elem_nodes[(size_t)j * N + e];
+            if (n < 0 || n >= V) continue;
+            cnt[n]++;
+            for (int k = 0; k < 4; k++) out[(size_t)k * V + n] += ruvp[k];
+        }
+    }
+    for (int n = 0; n < V; n++) {
+        if (cnt[n] != 0)
+            for (int k = 0; k < 4; k++) out[(size_t)k * V + n] /= cnt[n];
+        const double rho = out[n], u = out[(size_t)V + n], v = out[2 * (size_t)V + n], p = out[3 * (size_t)V + n];
+        out[4 * (size_t)V + n] = (p - p_inf) / pdyn_inf;
+        const double V2 = u * u + v * v;
+        const double a2 = gamma * p / rho;
+        out[5 * (size_t)V + n] = sqrt(V2 / a2);
+    }
+    free(cnt);
+}
+
+void om_boundary_forces(int NB, const int* set_off, const int* set_list, const int* bc_type, int E,
+                        const int* edge_nodes, const double* edge_normal, const double* edge_len,
+                        const double* Cp, double ref_area, double* cd, double* cl, double* cd_wall,
+                        double* cl_wall) {
+    const double one_on_Sref = 1 / ref_area;
+    double dw = 0.0, lw = 0.0;
+    for (int b = 0; b < NB; b++) {
+        double CD = 0.0, CL = 0.0;
+        for (int k = set_off[b]; k < set_off[b + 1]; k++) {
+            const int e = set_list[k];
+            const int n0 = edge_nodes[e], n1 = edge_nodes[(size_t)E + e];
+            const double c = 0.5 * (Cp[n0] + Cp[n1]);
+            const double dC = c * one_on_Sref * edge_len[e];
+            CD += dC * edge_normal[e];
+            CL += dC * edge_normal[(size_t)E + e];
+        }
+        cd[b] = CD;
+        cl[b] = CL;
+        /* _BC_wall_nonViscous, _BC_wall_adiabat, _BC_wall_isothermal (Constexpr.h:40-42) */
+        if (bc_type[b] == 6001 || bc_type[b] == 6002 || bc_type[b] == 6003) {
+            dw += CD;
+            lw += CL;
+        }
+    }
+    *cd_wall = dw;
+    *cl_wall = lw;
+}
+
+/* getColor_device (CudaGrid_kernels.cu:24-66) with the map of CudaGrid.cpp:31-37 */
+static void om_colour_of(float x, float* rgb) {
+    static const float map[5][4] = {{1.0f, 0.0f, 0.0f, 0.00f}, {1.0f, 1.0f, 0.0f, 0.25f}, {0.0f, 1.0f, 0.0f, 0.50f},
+                                    {0.0f, 0.0f, 1.0f, 0.75f}, {1.0f, 0.0f, 1.0f, 1.00f}};
+    if (x < 0.0f) x = 0.0f;
+    if (x > 1.0f) x = 1.0f;
+    for (int i = 0; i < 4; i++) {
+        if (x >= map[i][3] && x <= map[i + 1][3]) {
+            const float t0 = map[i][3], t1 = map[i + 1][3];
+            const float n = (x - t0) / (t1 - t0);
+            const float omn = 1 - n;
+            const float omn2 = omn * omn, omn3 = omn2 * omn;
+            const float n2 = n * n, n3 = n2 * n;
+            for (int k = 0; k < 3; k++) {
+                const float c0 = map[i][k], c1 = map[i + 1][k];
+                const float cm = 0.5f * (c0 + c1);
+                rgb[k] = omn3 * c0 + 3 * omn2 * n * cm + 3 * omn * n2 * cm + n3 * c1;
+            }
+            return;
+        }
+    }
+    rgb[0] = 252.0f / 255.0f;
+    rgb[1] = 3.0f / 255.0f;
+    rgb[2] = 253.0f / 255.0f;
+}
+
+/* accumulateElementDataToNodeData_k, divideNodeData_k, nodeDataToVertexColor_k
+ * (CudaGrid_kernels.cu:79-130), run in cell order: the max it takes is the same in
+ * any order except for NaN */
+void om_colour_nodes(int N, int V, const int* elem_nodes, const double* U, float range_lo, float range_hi,
+                     float* rgb, float* node_value) {
+    int* cnt = (int*)calloc((size_t)(V > 0 ? V : 1), sizeof(int));
+    for (int e = 0; e < N; e++)
+        for (int j = 0; j < 3; j++) cnt[elem_nodes[(size_t)j * N + e]]++;
+    for (int n = 0; n < V; n++) node_value[n] = 0.0f;
+    for (int e = 0; e < N; e++)
+        for (int j = 0; j < 3; j++) {
+            const int n = elem_nodes[(size_t)j * N + e];
+            float x = (float)U[e];
+            x *= cnt[n];
+            const float v = node_value[n];
+            node_value[n] = (v > x) ? v : x;
+        }
+    for (int n = 0; n < V; n++) {
+        float div = (float)(1.0 / cnt[n]);
+        if (div > 1e5) div = 1.0f;
+        node_value[n] *= div;
+        const float len = fabsf(range_hi - range_lo);
+        const float x = (len == 0) ? 0.0f : (node_value[n] - range_lo) / len;
+        om_colour_of(x, rgb + 3 * (size_t)n);
+    }
+    free(cnt);
+}

@@ -66,6 +66,25 @@ int om_restrict(const om_mesh* m, const om_params* p, double* U);
 int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* t, double* dts, double* last_rhs);
 /* Residual norm of an RHS field: norm 0 = L-infinity, 1 = L1, 2 = L2 (per variable). */
 void om_residual(const om_mesh* m, const double* rhs, int norm, double* out4);
+/* Node values for the Tecplot writers, FieldWriter::update_nodeField
+ * (FVMR/src/output/FieldWriter.cpp:364-453): per node the mean of its cells'
+ * U2ruvp values summed in cell order, then Cp against (p_inf, pdyn_inf) and Ma.
+ * elem_nodes [4][N] (slot 3 ignored), U [4][N]; out [6][V] = rho u v p Cp Ma. */
+void om_node_field(int N, int V, const int* elem_nodes, const double* U, double gamma, double p_inf,
+                   double pdyn_inf, double* out);
+/* ReferenceData::calculate_edgeSet_force (FieldWriter.cpp:175-210) per boundary
+ * set, the sets' edges in set order (set_off [NB+1], set_list), and the sums
+ * over wall sets (HistData::set_CDCL_wall, FieldWriter.cpp:611-632). */
+void om_boundary_forces(int NB, const int* set_off, const int* set_list, const int* bc_type, int E,
+                        const int* edge_nodes, const double* edge_normal, const double* edge_len,
+                        const double* Cp, double ref_area, double* cd, double* cl, double* cd_wall,
+                        double* cl_wall);
+/* The GUI's field colouring (FVMR/src/gui/cuda/CudaGrid_kernels.cu:24-130) in
+ * float arithmetic: node value = max over the node's cells of rho x count,
+ * times 1/count; colour through the five-point map of CudaGrid.cpp:31-37.
+ * rgb [V][3], node_value [V]. */
+void om_colour_nodes(int N, int V, const int* elem_nodes, const double* U, float range_lo, float range_hi,
+                     float* rgb, float* node_value);
 /* Host threads for the per-cell and per-edge loops (results do not depend on
  * the count: every output value is computed by one thread in the reference's
  * order).  n <= 0 keeps the current count; returns the count in use. */

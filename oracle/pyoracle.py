@@ -62,6 +62,15 @@ def lib():
         L.om_residual.argtypes = [ctypes.POINTER(OmMesh), dp, ctypes.c_int, dp]
         L.om_ruvp_from_mach.argtypes = [ctypes.c_double] * 6 + [dp]
         L.om_set_threads.argtypes = [ctypes.c_int]
+        ip, fp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)
+        L.om_node_field.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, dp]
+        L.om_node_field.restype = None
+        L.om_boundary_forces.argtypes = [ctypes.c_int, ip, ip, ip, ctypes.c_int, ip, dp, dp, dp, ctypes.c_double,
+                                         dp, dp, dp, dp]
+        L.om_boundary_forces.restype = None
+        L.om_colour_nodes.argtypes = [ctypes.c_int, ctypes.c_int, ip, dp, ctypes.c_float, ctypes.c_float, fp, fp]
+        L.om_colour_nodes.restype = None
         L.om_set_threads.restype = ctypes.c_int
         L.om_set_threads(int(os.environ.get("FVM_ORACLE_THREADS", "1")))
         _lib = L
@@ -75,6 +84,52 @@ def set_threads(n):
 
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def node_field(elem_nodes, U, V, gamma, inf):
+    """om_node_field: (6, V) node values; elem_nodes (4, N) int32, U (4, N), inf = (rho, u, v, p)."""
+    elem_nodes = np.ascontiguousarray(elem_nodes, dtype=np.int32)
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    N = U.shape[1]
+    p_inf = float(inf[3])
+    pdyn = 0.5 * float(inf[0]) * (float(inf[1]) * float(inf[1]) + float(inf[2]) * float(inf[2]))
+    out = np.empty((6, V))
+    lib().om_node_field(N, V, _ip(elem_nodes), _dp(U), float(gamma), p_inf, pdyn, _dp(out))
+    return out
+
+
+def boundary_forces(set_off, set_list, bc_type, edge_nodes, edge_normal, edge_len, Cp, ref_area):
+    """om_boundary_forces: (CD[NB], CL[NB], CD_wall, CL_wall)."""
+    set_off = np.ascontiguousarray(set_off, dtype=np.int32)
+    set_list = np.ascontiguousarray(set_list, dtype=np.int32)
+    bc_type = np.ascontiguousarray(bc_type, dtype=np.int32)
+    edge_nodes = np.ascontiguousarray(edge_nodes, dtype=np.int32)
+    E = edge_nodes.shape[1]
+    NB = len(bc_type)
+    cd, cl = np.empty(NB), np.empty(NB)
+    dw, lw = ctypes.c_double(), ctypes.c_double()
+    lib().om_boundary_forces(NB, _ip(set_off), _ip(set_list), _ip(bc_type), E, _ip(edge_nodes),
+                             _dp(np.ascontiguousarray(edge_normal, dtype=np.float64)),
+                             _dp(np.ascontiguousarray(edge_len, dtype=np.float64)),
+                             _dp(np.ascontiguousarray(Cp, dtype=np.float64)), float(ref_area), _dp(cd), _dp(cl),
+                             ctypes.byref(dw), ctypes.byref(lw))
+    return cd, cl, dw.value, lw.value
+
+
+def colour_nodes(elem_nodes, U, V, lo, hi):
+    """om_colour_nodes: (rgb (V, 3) float32, node values (V,) float32)."""
+    elem_nodes = np.ascontiguousarray(elem_nodes, dtype=np.int32)
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    rgb = np.empty((V, 3), dtype=np.float32)
+    val = np.empty(V, dtype=np.float32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib().om_colour_nodes(U.shape[1], V, _ip(elem_nodes), _dp(U), float(lo), float(hi), rgb.ctypes.data_as(fp),
+                          val.ctypes.data_as(fp))
+    return rgb, val
 
 
 def ruvp_from_mach(Ma, aoa, T0, p0, gamma, R):

@@ -50,9 +50,18 @@ def test_driver_matches_direct_stepping(tmp_path):
     t2 = s.step(0.0, p.T_end, 30)
     assert np.array_equal(s.get_state(), U) and t2 == t
     hist = open(os.path.join(d, "out", "jv_hist.dat")).read().split("\n")
-    assert hist[0].startswith("VARIABLES") and [int(l.split()[0]) for l in hist[1:] if l] == [1, 5, 10, 15, 20,
-                                                                                           25, 30]
+    assert hist[0] == 'title= "tecplot hist file"' and hist[1].startswith('variables= "Iteration"')
+    assert hist[2].startswith("zone")
+    rows = [l.split() for l in hist[3:] if l]
+    assert [int(r[0]) for r in rows] == [1, 5, 10, 15, 20, 25, 30] and all(len(r) == 8 for r in rows)
     assert "step = 10" in r.stdout and "step = 30" in r.stdout
+    # Tecplot volume files at step 1 and at the stop, the boundary file overwritten in place
+    out = os.path.join(d, "out")
+    for f in ("jv[0001].dat", "jv[0030].dat", "jv_tec_boundary.dat"):
+        assert os.path.getsize(os.path.join(out, f)) > 0, f
+    vol = open(os.path.join(out, "jv[0030].dat")).read().split("\n")
+    assert vol[1] == 'variables= "x", "y", "rho", "u", "v", "p", "Ma"' and f"nodes= {m.V}" in vol[2]
+    assert np.allclose([float(x) for x in vol[3].split()[2:6]], s.node_field()[:4, 0], rtol=1e-6)
 
 
 def test_restart_continues_bit_for_bit(tmp_path):
