@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--n", type=int, default=N_SIDE, help="cells per side of the square (default 1448)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=["vortex_large", "batch", "adjoint"], default="vortex_large",
+    ap.add_argument("--workload", choices=["vortex_large", "batch", "adjoint", "output"], default="vortex_large",
                     help="batch: many cylinder instances in one persistent launch per stage vs the same "
                          "instances stepped one after another through the plain path; adjoint: the discrete "
                          "adjoint through K SSP-RK3 steps on the 256x256 jittered vortex")
@@ -206,6 +206,49 @@ def run_batch(args):
             "sequential_plain": {"value": seq, "ms_per_step": ms_seq / args.steps,
                                  "kernel_launches_per_step": launches_seq / args.steps},
             "speedup_vs_sequential": ms_seq / ms_batch}
+    print(json.dumps(line), flush=True)
+
+
+def run_output(args):
+    """Field output on the 1448x1448 mesh: the node-value kernel (FieldWriter::update_nodeField)
+    and the colouring kernel (the GUI's cell -> node -> colour), device-timed, against HBM."""
+    import torch
+    torch.cuda.set_device(0)
+    import cfd_solver_2d_gpu_gb300 as fv
+    with tempfile.TemporaryDirectory() as d:
+        tp, su2, _ = workload(args, d)
+        p = fv.Params.from_toml(tp)
+        mesh = fv.Mesh.read_su2(su2, p)
+        s = fv.GPUSolver2(mesh, p)
+        s.step(0.0, p.T_end, 2)
+        N, V = mesh.N, mesh.V
+        s.output_timed(args.warmup)
+        reps = max(args.steps, 10)
+        with ClockSampler(0) as clk:
+            ms_nf, ms_col = s.output_timed(reps)
+        t0 = time.perf_counter()
+        path = os.path.join(d, "vol.dat")
+        s.write_tecplot_volume(path, 1.0)
+        t_write = time.perf_counter() - t0
+        size = os.path.getsize(path)
+    peak, peak_kind = measured_peaks()
+    # compulsory bytes: node values = the cells' primitives (read U 32 N, write 32 N) + the node
+    # gather (lists 4 (V + 1) + 12 N, primitives 32 N, outputs 48 V); colouring reads U once
+    nf_bytes = 64 * N + 4 * (V + 1) + 12 * N + 32 * N + 48 * V
+    col_bytes = 4 * (V + 1) + 12 * N + 32 * N + 16 * V
+    nf_ms, col_ms = ms_nf / reps, ms_col / reps
+    line = {"metric": "node values/s (field output, 1 GB300)", "value": V / (nf_ms / 1e3), "unit": "nodes/s",
+            "n_gpus": 1, "steps": reps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (generated mesh and initial field of the configuration's shape)",
+            "config": {"workload": f"node values and colouring of the 1448x1448 jittered vortex ({N} cells, {V} nodes)"},
+            "clocks": clk.summary(), "gpu_launches": 3 * reps,
+            "roofline": {"bound": "hbm", "kernel": "k_cell_ruvp + k_node_field", "achieved": nf_bytes / (nf_ms / 1e3) / 1e9,
+                         "peak": peak, "unit": "GB/s", "frac": nf_bytes / (nf_ms / 1e3) / 1e9 / peak,
+                         "algorithmic_bytes_per_launch": nf_bytes, "avg_launch_ms": nf_ms, "peak_source": peak_kind},
+            "colouring": {"value": V / (col_ms / 1e3), "unit": "nodes/s", "avg_launch_ms": col_ms,
+                          "achieved_gbs": col_bytes / (col_ms / 1e3) / 1e9,
+                          "frac": col_bytes / (col_ms / 1e3) / 1e9 / peak},
+            "tecplot_volume_write": {"seconds": t_write, "bytes": size, "MB_per_s": size / t_write / 1e6}}
     print(json.dumps(line), flush=True)
 
 
@@ -396,6 +439,10 @@ def main():
     if args.workload == "adjoint" and args.impl == "ours":
         if rank == 0:
             run_adjoint(args)
+        return
+    if args.workload == "output" and args.impl == "ours":
+        if rank == 0:
+            run_output(args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -131,6 +131,7 @@ def lib():
             "fvgb_colour_nodes": (i, [v, d, d, ctypes.POINTER(ctypes.POINTER(ctypes.c_float)),
                                       ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
             "fvgb_num_nodes": (i, [v, ip]),
+            "fvgb_output_timed": (i, [v, i, dp, dp]),
             "fvgb_last_error": (c, []),
             "fvgb_version": (c, []),
         }
@@ -377,6 +378,12 @@ class GPUSolver2:
         _check(lib().fvgb_colour_nodes(self._h, float(range_lo), float(range_hi), ctypes.byref(dev),
                                        rgb.ctypes.data_as(fp), val.ctypes.data_as(fp)))
         return rgb, val, ctypes.cast(dev, ctypes.c_void_p).value
+
+    def output_timed(self, reps):
+        """Device ms of reps node-value launches and of reps colouring launches."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(lib().fvgb_output_timed(self._h, int(reps), ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def update_residual_vector(self, norm=0):
         out = np.zeros(4)

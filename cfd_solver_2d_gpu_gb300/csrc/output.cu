@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstdio>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -38,28 +39,36 @@ struct OutputState {
     double* d_field = nullptr;    // [6][V]: rho u v p Cp Ma
     float* d_rgb = nullptr;       // [V][3]
     float* d_node_value = nullptr;
+    d4* d_cell_ruvp = nullptr;    // [N]: each cell's rho u v p, computed once per call
     std::vector<double> h_field;  // host copy of d_field
 };
 
 namespace dev {
 
-__global__ void __launch_bounds__(256) k_node_field(const d4* __restrict__ U, const int* __restrict__ ptr,
-                                                    const int* __restrict__ cells, int V, double gm1, double gamma,
+// U2ruvp_host once per cell: rho, U1/U0, U2/U0, rho (gamma-1) (U3/U0 - (u u + v v) 0.5)
+__global__ void __launch_bounds__(256) k_cell_ruvp(const d4* __restrict__ U, int N, double gm1,
+                                                   d4* __restrict__ ruvp) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const d4 u = ld4(&U[c]);
+    const double uu = __ddiv_rn(u.y, u.x), vv = __ddiv_rn(u.z, u.x);
+    const double q = __dmul_rn(__dadd_rn(__dmul_rn(uu, uu), __dmul_rn(vv, vv)), 0.5);
+    ruvp[c] = mk4(u.x, uu, vv, __dmul_rn(__dmul_rn(u.x, gm1), __dsub_rn(__ddiv_rn(u.w, u.x), q)));
+}
+
+__global__ void __launch_bounds__(256) k_node_field(const d4* __restrict__ ruvp, const int* __restrict__ ptr,
+                                                    const int* __restrict__ cells, int V, double gamma,
                                                     double p_inf, double pdyn_inf, double* __restrict__ f) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= V) return;
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
     const int b = ptr[n], e = ptr[n + 1];
     for (int k = b; k < e; k++) {
-        const d4 u = ld4(&U[cells[k]]);
-        // U2ruvp_host: rho, U1/U0, U2/U0, rho (gamma-1) (U3/U0 - (u u + v v) 0.5)
-        const double uu = __ddiv_rn(u.y, u.x), vv = __ddiv_rn(u.z, u.x);
-        const double q = __dmul_rn(__dadd_rn(__dmul_rn(uu, uu), __dmul_rn(vv, vv)), 0.5);
-        const double pp = __dmul_rn(__dmul_rn(u.x, gm1), __dsub_rn(__ddiv_rn(u.w, u.x), q));
-        s0 = __dadd_rn(s0, u.x);
-        s1 = __dadd_rn(s1, uu);
-        s2 = __dadd_rn(s2, vv);
-        s3 = __dadd_rn(s3, pp);
+        const d4 w = ld4(&ruvp[cells[k]]);
+        s0 = __dadd_rn(s0, w.x);
+        s1 = __dadd_rn(s1, w.y);
+        s2 = __dadd_rn(s2, w.z);
+        s3 = __dadd_rn(s3, w.w);
     }
     if (e > b) {
         const double c = (double)(e - b);
@@ -195,6 +204,7 @@ void Solver::release_output() {
     cudaFree(out->d_field);
     cudaFree(out->d_rgb);
     cudaFree(out->d_node_value);
+    cudaFree(out->d_cell_ruvp);
     delete out;
     out = nullptr;
 }
@@ -217,6 +227,7 @@ static int output_ready(Solver& s) {
     OK_(cudaMalloc(&o->d_field, sizeof(double) * 6 * (size_t)V));
     OK_(cudaMalloc(&o->d_rgb, sizeof(float) * 3 * (size_t)V));
     OK_(cudaMalloc(&o->d_node_value, sizeof(float) * (size_t)V));
+    OK_(cudaMalloc(&o->d_cell_ruvp, sizeof(d4) * (size_t)(N > 0 ? N : 1)));
     OK_(cudaMemcpyAsync(o->d_node_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice, s.stream));
     OK_(cudaMemcpyAsync(o->d_node_cells, cells.data(), sizeof(int) * cells.size(), cudaMemcpyHostToDevice, s.stream));
     OK_(cudaStreamSynchronize(s.stream));
@@ -230,21 +241,28 @@ static void farfield_reference(const fvgb_params& p, double* p_inf, double* pdyn
     *pdyn = 0.5 * p.inf[0] * V2;
 }
 
+static void launch_node_field(Solver& s, double p_inf, double pdyn) {
+    const int V = s.om.V, N = s.N;
+    if (N > 0) dev::k_cell_ruvp<<<(N + 255) / 256, 256, 0, s.stream>>>(s.d_U, N, s.p.gamma - 1, s.out->d_cell_ruvp);
+    if (V > 0)
+        dev::k_node_field<<<(V + 255) / 256, 256, 0, s.stream>>>(s.out->d_cell_ruvp, s.out->d_node_ptr,
+                                                                 s.out->d_node_cells, V, s.p.gamma, p_inf, pdyn,
+                                                                 s.out->d_field);
+    s.launches += 2;
+}
+
 static int node_field(Solver& s) {
     int rc = output_ready(s);
     if (rc) return rc;
     const int V = s.om.V;
     double p_inf, pdyn;
     farfield_reference(s.p, &p_inf, &pdyn);
-    if (V > 0)
-        dev::k_node_field<<<(V + 255) / 256, 256, 0, s.stream>>>(s.d_U, s.out->d_node_ptr, s.out->d_node_cells, V,
-                                                                 s.p.gamma - 1, s.p.gamma, p_inf, pdyn, s.out->d_field);
+    launch_node_field(s, p_inf, pdyn);
     OK_(cudaGetLastError());
     s.out->h_field.resize(6 * (size_t)V);
     OK_(cudaMemcpyAsync(s.out->h_field.data(), s.out->d_field, sizeof(double) * 6 * (size_t)V, cudaMemcpyDeviceToHost,
                         s.stream));
     OK_(cudaStreamSynchronize(s.stream));
-    s.launches += 1;
     return 0;
 }
 
@@ -286,7 +304,7 @@ struct Text {
     }
     void put(const char* s) {
         buf += s;
-        if (buf.size() > (1u << 22)) flush();
+        if (f && buf.size() > (1u << 22)) flush();
     }
     void e(double x) {  // std::scientific, default precision: %e
         char t[40];
@@ -331,15 +349,39 @@ static int write_volume(Solver& s, const char* path, const char* title, double t
                   "zonetype= fequadrilateral, solutiontime= %e\n",
                   title, variable_names(preset), s.om.V, s.N, t);
     o.put(line);
-    for (int n = 0; n < s.om.V; n++) node_line(o, s, n, preset);
-    const int N = s.N;
-    for (int c = 0; c < N; c++) {
-        const int a = s.om.elem_nodes[c] + 1, b = s.om.elem_nodes[(size_t)N + c] + 1,
-                  d = s.om.elem_nodes[2 * (size_t)N + c] + 1;
-        std::snprintf(line, sizeof line, "%d %d %d %d\n", a, b, d, d);
-        o.put(line);
-    }
     o.flush();
+    // the node lines, then the cells' node lists: formatted in chunks on host threads, written in order
+    const int V = s.om.V, N = s.N;
+    const long long total = (long long)V + N;
+    const int nthreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const long long chunk = 1 << 16;
+    for (long long base = 0; base < total; base += chunk * nthreads) {
+        std::vector<std::string> parts(nthreads);
+        std::vector<std::thread> pool;
+        for (int w = 0; w < nthreads; w++) {
+            const long long lo = base + (long long)w * chunk, hi = std::min(total, lo + chunk);
+            if (lo >= hi) break;
+            pool.emplace_back([&, w, lo, hi] {
+                Text part;
+                char l[64];
+                for (long long i = lo; i < hi; i++) {
+                    if (i < V) {
+                        node_line(part, s, (int)i, preset);
+                    } else {
+                        const int c = (int)(i - V);
+                        const int a = s.om.elem_nodes[c] + 1, b = s.om.elem_nodes[(size_t)N + c] + 1,
+                                  d = s.om.elem_nodes[2 * (size_t)N + c] + 1;
+                        std::snprintf(l, sizeof l, "%d %d %d %d\n", a, b, d, d);
+                        part.buf += l;
+                    }
+                }
+                parts[w] = std::move(part.buf);
+            });
+        }
+        for (auto& th : pool) th.join();
+        for (auto& part : parts)
+            if (!part.empty()) std::fwrite(part.data(), 1, part.size(), o.f);
+    }
     const bool ok = std::ferror(o.f) == 0;
     if (std::fclose(o.f) != 0 || !ok) return fail(FVGB_ERR_IO, std::string("write failed: ") + path);
     return 0;
@@ -437,5 +479,42 @@ extern "C" int fvgb_colour_nodes(fvgb_handle* h, double range_lo, double range_h
 extern "C" int fvgb_num_nodes(fvgb_handle* h, int* V) {
     if (!h || !V) return fail(FVGB_ERR_ARG, "null argument");
     *V = h->s.om.V;
+    return 0;
+}
+
+// reps launches of each output kernel on the handle's stream, bracketed by CUDA events
+extern "C" int fvgb_output_timed(fvgb_handle* h, int reps, double* ms_node_field, double* ms_colour) {
+    if (!h || reps <= 0) return fail(FVGB_ERR_ARG, "bad arguments");
+    Solver& s = h->s;
+    cudaSetDevice(s.p.device);
+    int rc = output_ready(s);
+    if (rc) return rc;
+    const int V = s.om.V;
+    if (V == 0) return fail(FVGB_ERR_ARG, "mesh has no nodes");
+    double p_inf, pdyn;
+    farfield_reference(s.p, &p_inf, &pdyn);
+    cudaEvent_t a, b, c;
+    OK_(cudaEventCreate(&a));
+    OK_(cudaEventCreate(&b));
+    OK_(cudaEventCreate(&c));
+    const int grid = (V + 255) / 256;
+    OK_(cudaEventRecord(a, s.stream));
+    for (int i = 0; i < reps; i++) launch_node_field(s, p_inf, pdyn);
+    OK_(cudaEventRecord(b, s.stream));
+    for (int i = 0; i < reps; i++)
+        dev::k_colour<<<grid, 256, 0, s.stream>>>(s.d_U, s.out->d_node_ptr, s.out->d_node_cells, V, 0.5f, 1.5f,
+                                                  s.out->d_rgb, s.out->d_node_value);
+    OK_(cudaEventRecord(c, s.stream));
+    OK_(cudaEventSynchronize(c));
+    OK_(cudaGetLastError());
+    float t1 = 0, t2 = 0;
+    OK_(cudaEventElapsedTime(&t1, a, b));
+    OK_(cudaEventElapsedTime(&t2, b, c));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaEventDestroy(c);
+    s.launches += (long long)reps;
+    if (ms_node_field) *ms_node_field = t1;
+    if (ms_colour) *ms_colour = t2;
     return 0;
 }

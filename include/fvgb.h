@@ -231,6 +231,9 @@ int fvgb_write_tecplot_boundary(fvgb_handle* h, const char* path, double t, int 
 int fvgb_colour_nodes(fvgb_handle* h, double range_lo, double range_hi, float** rgb_dev, float* rgb_host,
                       float* node_value_host);
 int fvgb_num_nodes(fvgb_handle* h, int* V);
+/* reps launches of the node-value kernel, then of the colouring kernel, each
+ * series bracketed by CUDA events on the handle's stream (device ms per series). */
+int fvgb_output_timed(fvgb_handle* h, int reps, double* ms_node_field, double* ms_colour);
 
 /* ---- discrete adjoint ------------------------------------------------------
  * No counterpart in the reference.  Reverse-mode derivative of K steps of the

@@ -17,6 +17,12 @@
 //   ssprk3     Shu-Osher SSP-RK3 built the same way (new code 3104)
 //   rhs        one calculateFunctionF on the initial field, plus its dt
 //   mesh       assembly and initial field only
+//   output     nsteps forward-Euler steps, then the reference's own field output of
+//              the final state: FieldWriter::update_nodeField (node values dumped),
+//              write_tecplot_volume_file / write_tecplot_boundary_file and one
+//              write_tecplot_hist_file line (residuals 1, 2, 3, 4), written to
+//              <out>.volume.dat, <out>.boundary.dat and <out>.hist.dat
+//              (FVMR/src/output/FieldWriter.cpp:44-262, 364-453)
 //   continue   the newest pause_<basic.filename>[n].dat of the folder given in
 //              place of the mesh, read by ContinueFileReader::readContinueFile_1
 //              (FVMR/src/input/ContinueFileReader.cpp:19-158): mesh and field only
@@ -33,6 +39,7 @@
 #include "input/SU2MeshReader.h"
 #include "input/FieldInitializer.h"
 #include "input/ContinueFileReader.h"
+#include "output/FieldWriter.h"
 #include "solvers/GPUSolver2.h"
 #include "time/CIteration.h"
 #include "time/CalculateDt.h"
@@ -193,8 +200,8 @@ int main(int argc, char** argv) {
     std::vector<double> dts;
     std::vector<double> k1, k2, k3, Us;
     for (int step = 0; step < nsteps; step++) {
-        if (mode == "euler" || mode == "rk3lit") {
-            GlobalPara::time::time_advance = (mode == "euler") ? _EVO_explicit : _EVO_rk3;
+        if (mode == "euler" || mode == "rk3lit" || mode == "output") {
+            GlobalPara::time::time_advance = (mode == "rk3lit") ? _EVO_rk3 : _EVO_explicit;
             myfloat t0 = t;
             CIteration::iteration_host(t, T, &s);
             dts.push_back((double)(t - t0));
@@ -238,6 +245,25 @@ int main(int argc, char** argv) {
         U2NITS::Space::Restrict::modifyElementFieldU2d(s.element_host, s.elementField_host);
     }
     d.rows("U", s.elementField_host.U, 4, N);
+    if (mode == "output") {
+        // the writers read ruvp: refresh it from the final state
+        CIteration::update_host_ruvp_Uold(s.elementField_host.U, s.elementField_host.ruvp, s.elementField_host.Uold, N,
+                                          GlobalPara::constant::gamma);
+        // the output schemes were read with input.toml and the node arrays allocated by
+        // GPUSolver2::allocateMemory (GPUSolver2.cpp:97)
+        FieldWriter* w = FieldWriter::getInstance();
+        w->update_nodeField();
+        d.rows("node_ruvp", s.outputNodeField.ruvp, 4, V);
+        d.f64("node_Cp", std::vector<double>(s.outputNodeField.Cp.begin(), s.outputNodeField.Cp.end()));
+        d.f64("node_Ma", std::vector<double>(s.outputNodeField.Ma.begin(), s.outputNodeField.Ma.end()));
+        const std::string base = out;
+        w->write_tecplot_volume_file(t, base + ".volume.dat", "title", s.node_host, s.element_host, s.outputNodeField);
+        w->write_tecplot_boundary_file(t, base + ".boundary.dat", s.node_host, s.edge_host, s.outputNodeField,
+                                       s.boundary_host_new);
+        myfloat res[4] = {1, 2, 3, 4};
+        w->write_tecplot_hist_file(base + ".hist.dat", nsteps, t, res, s.edge_host, s.outputNodeField,
+                                   s.boundary_host_new);
+    }
     d.f64("dts", dts);
     std::vector<double> tt = {(double)t};
     d.f64("t", tt);

@@ -76,12 +76,6 @@ alignas(64) static unsigned char g_driver_storage[sizeof(U2NITS::CDriver)];
 U2NITS::CDriver* U2NITS::CDriver::getInstance() {
     return reinterpret_cast<U2NITS::CDriver*>(g_driver_storage);
 }
-alignas(64) static unsigned char g_writer_storage[sizeof(FieldWriter)];
-FieldWriter* FieldWriter::getInstance() { return reinterpret_cast<FieldWriter*>(g_writer_storage); }
-void FieldWriter::initialize_outputScheme_usingConfig() {}
-void FieldWriter::allocNodeFieldDataUsingOutputScheme(GPU::OutputNodeFieldSoA&, myint) {}
-void FieldWriter::freeNodeFieldData(GPU::OutputNodeFieldSoA&) {}
-void FieldWriter::update_nodeField() {}
 alignas(64) static unsigned char g_routine_storage[sizeof(RoutineController)];
 RoutineController* RoutineController::getInstance() {
     return reinterpret_cast<RoutineController*>(g_routine_storage);

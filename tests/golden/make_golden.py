@@ -108,6 +108,43 @@ def make_continue(d):
         print(f"{dst}: N={ref['sizes'][0]} ({os.path.getsize(dst) // 1024} KiB)")
 
 
+OUTPUT_DIR = os.path.join(HERE, "output")
+
+
+def output_cases(d):
+    """(name, toml text, su2 path, forward-Euler steps) of the field-output fixtures."""
+    T = cases.toml_text
+    return [
+        ("cylinder32_ns", T(equation=2, flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3101,
+                            CFL=0.5, ic_type=1, inf_mode=0, Ma=0.3, AoA=4.0, Re=100.0, ref_area=2.0),
+         cases.cylinder_mesh(32, 16, directory=d), 5),
+        ("jvortex24", T(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3101, CFL=0.5,
+                        inf=(1.0, 1.0, 0.3, 1.0)), cases.square_mesh(24, jitter=0.2, directory=d), 3),
+    ]
+
+
+def make_output(d):
+    """The reference's own field output (FieldWriter: node values, Tecplot volume and boundary
+    files, one hist line) after a few forward-Euler steps (oracle/_ref, output mode)."""
+    os.makedirs(OUTPUT_DIR, exist_ok=True)
+    for name, toml, su2, steps in output_cases(d):
+        tp = os.path.join(d, name + "_out.toml")
+        with open(tp, "w") as f:
+            f.write(toml)
+        base = os.path.join(d, name + "_out.bin")
+        ref = run_ref(REF, tp, su2, "output", steps, base)
+        gz = lambda path: np.frombuffer(gzip.compress(open(path, "rb").read(), mtime=0), dtype=np.uint8)
+        out = dict(U=ref["U"], t=ref["t"], node_ruvp=ref["node_ruvp"], node_Cp=ref["node_Cp"],
+                   node_Ma=ref["node_Ma"], volume_gz=gz(base + ".volume.dat"), boundary_gz=gz(base + ".boundary.dat"),
+                   hist=np.frombuffer(open(base + ".hist.dat", "rb").read(), dtype=np.uint8),
+                   toml=np.frombuffer(toml.encode(), dtype=np.uint8),
+                   su2_gz=np.frombuffer(gzip.compress(open(su2, "rb").read(), mtime=0), dtype=np.uint8),
+                   steps=np.array([steps]))
+        dst = os.path.join(OUTPUT_DIR, name + ".npz")
+        np.savez_compressed(dst, **out)
+        print(f"{dst}: N={ref['sizes'][0]} ({os.path.getsize(dst) // 1024} KiB)")
+
+
 def run_ref(binary, toml_path, su2, mode, steps, out):
     r = subprocess.run([binary, toml_path, su2, mode, str(steps), out], capture_output=True, text=True)
     if r.returncode != 0:
@@ -138,6 +175,7 @@ def main():
             np.savez_compressed(path, **out)
             print(f"{path}: N={rhs['sizes'][0]} {mode} x{steps} ({os.path.getsize(path) // 1024} KiB)")
         make_continue(d)
+        make_output(d)
 
 
 def load(name):
