@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(256) k_noalloc_flux(RefMesh m, const double* _
         uR = load_ref(U, m.N, R);
     }
     const dev::Prim wR = dev::to_prim(uR, g);
-    const d4 f = (FLUX == 2002) ? dev::roe_flux(wL, wR, nx, ny, len, g) : dev::llf_flux(uL, uR, wL, wR, nx, ny, len, g);
+    const d4 f = (FLUX == 2002) ? dev::roe_flux(wL, wR, uL, uR, nx, ny, len, g) : dev::llf_flux(uL, uR, wL, wR, nx, ny, len, g);
     F[e] = f.x;
     F[(size_t)m.E + e] = f.y;
     F[2 * (size_t)m.E + e] = f.z;

@@ -61,26 +61,28 @@ __device__ __forceinline__ bool is_nan(double x) {
     return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
 
-// 1/x: the hardware's approximate reciprocal refined by two Newton steps
-// (y <- y + y (1 - x y); each step squares the relative error), within ~1 ulp
-// of the correctly rounded value for normal x.
+// 1/x: the hardware's approximate reciprocal y (relative error e = 1 - x y,
+// |e| < 2^-22) refined by the cubic series 1/x = y (1 + e + e^2 + O(e^3)), one
+// fused multiply-add fewer than two Newton steps for the same accuracy: the
+// truncation y e^3 is below 2^-66, so the result is within ~1 ulp of the
+// correctly rounded value for normal x.
 __device__ __forceinline__ double rcp(double x) {
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    double e = fma(-x, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-x, y, 1.0);
-    return fma(y, e, y);
+    const double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
 }
 
-// U2ruvp_host, FVMR/src/math/PhysicalKernel.h:11-18
+// U2ruvp_host, FVMR/src/math/PhysicalKernel.h:11-18; the pressure as
+// (gamma-1) (rho E - (rho u u + rho v v)/2), equal to the reference's
+// rho (gamma-1) (E/rho - (u u + v v)/2) with four FP64 operations instead of six
 __device__ __forceinline__ Prim to_prim(const d4 U, const Gas& g) {
     Prim w;
     w.ir = rcp(U.x);
     w.r = U.x;
     w.u = U.y * w.ir;
     w.v = U.z * w.ir;
-    w.p = w.r * g.ga1 * (U.w * w.ir - (w.u * w.u + w.v * w.v) * 0.5);
+    w.p = g.ga1 * fma(-0.5, fma(U.y, w.u, U.z * w.v), U.w);
     return w;
 }
 
@@ -105,42 +107,44 @@ __device__ __forceinline__ d4 lin(const d4 U, const d4 gx, const d4 gy, double d
 }
 
 // ConvectRoeCommon2d + RoeDissapationTerm2d, FVMR/src/space/convection/Roe.cpp:380-538
-// (entropy fix off, static mesh)
-__device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, double nx, double ny, double area,
-                                            const Gas& g) {
-    const double unL = nx * L.u + ny * L.v, unR = nx * R.u + ny * R.v;
-    const double ruL = L.r * unL, ruR = R.r * unR;
-    const double V2L = L.u * L.u + L.v * L.v, V2R = R.u * R.u + R.v * R.v;
-    const double EL = L.p * L.ir, ER = R.p * R.ir;  // p/rho
-    const double HL = fma(g.gam_over_ga1, EL, 0.5 * V2L);
-    const double HR = fma(g.gam_over_ga1, ER, 0.5 * V2R);
+// (entropy fix off, static mesh).  L, R: the face states' primitive variables; UL, UR
+// the same states conserved.  Exact identities save FP64 work: the mass flux is
+// n . (rho u) from the momentum, the total enthalpy H = gamma/(gamma-1) p/rho + V^2/2
+// is (rho E + p)/rho, H - p/rho is rho E/rho, and with a > 0
+// (|un + a| + |un - a|)/2 = max(|un|, a), (|un + a| - |un - a|)/2 = un if |un| < a,
+// else a sgn(un).
+__device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, const d4 UL, const d4 UR, double nx, double ny,
+                                       double area, const Gas& g) {
+    const double ruL = fma(nx, UL.y, ny * UL.z), ruR = fma(nx, UR.y, ny * UR.z);
+    const double HL = (UL.w + L.p) * L.ir, HR = (UR.w + R.p) * R.ir;
     const double psum = L.p + R.p;
     // central part 0.5 (F_L + F_R).n, scaled by 0.5 area at the end
     d4 F = mk4(ruL + ruR, fma(ruL, L.u, fma(ruR, R.u, nx * psum)), fma(ruL, L.v, fma(ruR, R.v, ny * psum)),
                fma(ruL, HL, ruR * HR));
     // Roe averages: rm = sqrt(rR rL), rrorl = sqrt(rR/rL) = rR / rm
-    const double irm = rsqrt(R.r * L.r);
-    const double rm = (R.r * L.r) * irm;
+    const double prod = R.r * L.r;
+    const double irm = rsqrt(prod);
+    const double rm = prod * irm;
     const double rrorl = R.r * irm;
     const double w = rcp(rrorl + 1.0);
     const double um = fma(R.u, rrorl, L.u) * w;
     const double vm = fma(R.v, rrorl, L.v) * w;
     const double Hm = fma(HR, rrorl, HL) * w;
-    const double Vm2 = um * um + vm * vm;
-    const double am2 = g.ga1 * (Hm - 0.5 * Vm2);
+    const double Vm2 = fma(um, um, vm * vm);
+    const double am2 = g.ga1 * fma(-0.5, Vm2, Hm);
     const double iam = rsqrt(am2);
     const double am = am2 * iam;
-    const double un = um * nx + vm * ny;
-    const double eig1 = fabs(un), eig2 = fabs(un + am), eig3 = fabs(un - am);
-    const double dE = (HR - ER) - (HL - EL);
+    const double un = fma(um, nx, vm * ny);
+    const double eig1 = fabs(un);
+    const double astar = dmax(eig1, am);                                   // (eig2 + eig3) / 2
+    const double Mstar = (dlt(eig1, am) ? un : copysign(am, un)) * iam;   // (eig2 - eig3) / (2 am)
+    const double dE = fma(UR.w, R.ir, -UL.w * L.ir);                        // (HR - ER) - (HL - EL)
     const double Etm = fma(g.Etm_c, Vm2, Hm * g.inv_gamma);
     const double dW0 = R.r - L.r;
     const double du = R.u - L.u, dv = R.v - L.v;
     const double dW1 = fma(rm, du, dW0 * um);
     const double dW2 = fma(rm, dv, dW0 * vm);
     const double dW3 = fma(rm, dE, dW0 * Etm);
-    const double astar = (eig2 + eig3) * 0.5;
-    const double Mstar = (eig2 - eig3) * 0.5 * iam;
     const double dun = fma(nx, du, ny * dv);
     const double dp = R.p - L.p;
     const double ae = astar - eig1;
@@ -156,12 +160,13 @@ __device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, double nx, 
 }
 
 // LocalLaxFriedrichs, FVMR/src/space/convection/LocalLaxFriedrichs.cpp:4-47
+// (the mass flux and the total enthalpy from the conserved states, as in roe_flux)
 __device__ __forceinline__ d4 llf_flux(const d4 UL, const d4 UR, const Prim& L, const Prim& R,
                                             double nx, double ny, double length, const Gas& g) {
-    const double unL = nx * L.u + ny * L.v, unR = nx * R.u + ny * R.v;
-    const double ruL = L.r * unL, ruR = R.r * unR;
-    const double hl = g.gam_over_ga1 * L.p * L.ir + 0.5 * (L.u * L.u + L.v * L.v);
-    const double hr = g.gam_over_ga1 * R.p * R.ir + 0.5 * (R.u * R.u + R.v * R.v);
+    const double unL = fma(nx, L.u, ny * L.v), unR = fma(nx, R.u, ny * R.v);
+    const double ruL = fma(nx, UL.y, ny * UL.z), ruR = fma(nx, UR.y, ny * UR.z);
+    const double hl = (UL.w + L.p) * L.ir;
+    const double hr = (UR.w + R.p) * R.ir;
     const double aL = fabs(unL) + sqrt(g.gamma * L.p * L.ir);
     const double aR = fabs(unR) + sqrt(g.gamma * R.p * R.ir);
     const double lm = dmax(aL, aR);

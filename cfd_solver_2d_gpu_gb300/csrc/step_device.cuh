@@ -238,7 +238,7 @@ __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, c
         fL = face_state<false>(uL, gxL, gyL, 0, 0, g, wL);
         fR = face_state<false>(uR, gxR, gyR, 0, 0, g, wR);
     }
-    d4 flux = (FLUX == FLUX_ROE) ? roe_flux(wL, wR, nx, ny, len, g) : llf_flux(fL, fR, wL, wR, nx, ny, len, g);
+    d4 flux = (FLUX == FLUX_ROE) ? roe_flux(wL, wR, fL, fR, nx, ny, len, g) : llf_flux(fL, fR, wL, wR, nx, ny, len, g);
     if (NS) {
         // get_U_Gradient_mean / get_U_mean (ViscousFluxGPU.cu:7-87): averages of both sides
         const d4 ua = mk4(0.5 * (uL.x + uR.x), 0.5 * (uL.y + uR.y), 0.5 * (uL.z + uR.z), 0.5 * (uL.w + uR.w));
@@ -288,7 +288,7 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
         break;
     }
     const Prim wR = to_prim(fR, g);
-    d4 flux = (FLUX == FLUX_ROE) ? roe_flux(wL, wR, nx, ny, len, g) : llf_flux(fL, fR, wL, wR, nx, ny, len, g);
+    d4 flux = (FLUX == FLUX_ROE) ? roe_flux(wL, wR, fL, fR, nx, ny, len, g) : llf_flux(fL, fR, wL, wR, nx, ny, len, g);
     if (NS) viscous_flux(flux, uL, gxL, gyL, nx, ny, len, g);  // boundary: the L cell's values
     F[e] = flux;
 }
