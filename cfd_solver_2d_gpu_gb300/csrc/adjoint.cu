@@ -10,17 +10,19 @@
 // positivity pass is assumed inactive (the forward reports whether it acted).
 //
 // Memory: checkpoints of U every S = ceil(K / n_checkpoints) steps; during the
-// reverse sweep each segment is recomputed once, keeping U_0, U_1, U_2 of each
-// of its steps, so the sweep costs one extra forward pass and O((K/S + 3 S) N)
-// states (sqrt(K) checkpoints: O(sqrt(K) N)).
+// reverse sweep each segment is recomputed once, keeping per step U_0, U_1, U_2,
+// the stages' residuals and edge tapes, so the sweep costs one extra forward pass
+// and O(K/S N + S (6 N + 117 E)) doubles (sqrt(K) checkpoints: O(sqrt(K) N)).
 //
 // Kernels of one stage VJP (all gathers, no atomics: deterministic):
-//   k_adj_edge     per edge: face states, mu = seed-weighted flux adjoint, flux VJP
+//   k_adj_edge     per edge: mu = seed-weighted flux adjoint, flux VJP from the stage's tape
 //   k_adj_cell     per cell: gather the face-state adjoints of its edges; limiter + LSQ VJP
 //   k_adj_combine  per cell: gather the neighbours' LSQ adjoints; the stage's RK combination;
 //                  block partials of lam_s . R_s (the time step's adjoint)
 // and once a step k_adj_dt.  The recorded forward keeps, per stage, the input state, the
-// limited gradients and the residual R_s, so no stage recomputes them.
+// residual R_s and the edge tape (face states and Roe intermediates, step_device.cuh), so
+// the reverse sweep recomputes none of them: on this part FP64 issue, not memory, is
+// scarce (39 doubles a stage per edge; 3.9 GB for 23 steps of the 256x256 mesh).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,66 +39,53 @@ namespace fvgb {
 namespace dev {
 
 // ---- per edge --------------------------------------------------------------
-// 128-thread blocks: ~156 registers a thread leave room for three blocks per SM
+// 128-thread blocks: ~126 registers a thread leave room for four blocks per SM
 constexpr int kEdgeThreads = 128;
 
-template <bool LINEAR>
-__global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(const d4* __restrict__ U, const d4* __restrict__ Gx,
-                                                  const d4* __restrict__ Gy, MeshView m, Gas g,
-                                                  const d4* __restrict__ lam, const int* __restrict__ e_rlist,
-                                                  d4* __restrict__ aL, d4* __restrict__ aR,
-                                                  int* __restrict__ aflag) {
+// mu = dLoss/dF_e (F_e enters R_L with +1/-vol and, when e is in R's edge list, R_R with
+// -1/-vol), then the flux VJP from the stage's recorded tape: the face states and the
+// Roe intermediates are read, not recomputed
+__global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView m, Gas g,
+                                                           const d4* __restrict__ lam,
+                                                           const int* __restrict__ e_rlist, d4* __restrict__ aL,
+                                                           d4* __restrict__ aR) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < m.E) {
-        const int L = __ldg(&m.e_L[e]), R = __ldg(&m.e_R[e]);
-        const double* gm = &m.e_geom[(size_t)e * 8];
-        const double nx = __ldg(&gm[0]), ny = __ldg(&gm[1]), len = __ldg(&gm[2]);
-        // mu = dLoss/dF_e: F_e enters R_L with +1/-vol and, when e is in R's edge list, R_R with -1/-vol
-        const double mL = __ldg(&m.c_mvol[L]);
-        const d4 lL = ld4(&lam[L]);
-        d4 mu = mk4(mL * lL.x, mL * lL.y, mL * lL.z, mL * lL.w);
-        if (__ldg(&e_rlist[e])) {
-            const double mR = __ldg(&m.c_mvol[R]);
-            const d4 lR = ld4(&lam[R]);
-            mu = mk4(mu.x - mR * lR.x, mu.y - mR * lR.y, mu.z - mR * lR.z, mu.w - mR * lR.w);
-        }
-        const d4 uL = ld4(&U[L]);
-        d4 gxL = mk4(0, 0, 0, 0), gyL = gxL;
-        if (LINEAR) {
-            gxL = ld4(&Gx[L]);
-            gyL = ld4(&Gy[L]);
-        }
-        Prim wL;
-        bool usedL, usedR = false;
-        const d4 fL = face_state_used<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL, usedL);
-        d4 bfL = mk4(0, 0, 0, 0), bfR = mk4(0, 0, 0, 0);
-        Prim bwL{}, bwR{};
-        if (e < m.E_int) {
-            const d4 uR = ld4(&U[R]);
-            d4 gxR = mk4(0, 0, 0, 0), gyR = gxR;
-            if (LINEAR) {
-                gxR = ld4(&Gx[R]);
-                gyR = ld4(&Gy[R]);
-            }
-            Prim wR;
-            const d4 fR = face_state_used<LINEAR>(uR, gxR, gyR, __ldg(&gm[6]), __ldg(&gm[7]), g, wR, usedR);
-            roe_flux_vjp(wL, wR, nx, ny, len, g, mu, bwL, bwR);
-            to_prim_vjp(fR, wR, g, bwR, bfR);
-            to_prim_vjp(fL, wL, g, bwL, bfL);
-        } else {  // slip wall / symmetry: the ghost is a function of the L face state
-            const d4 fR = ghost_slip(fL, wL, nx, ny);
-            const Prim wR = to_prim(fR, g);
-            roe_flux_vjp(wL, wR, nx, ny, len, g, mu, bwL, bwR);
-            d4 bgR = mk4(0, 0, 0, 0);
-            to_prim_vjp(fR, wR, g, bwR, bgR);
-            ghost_slip_vjp(fL, wL, nx, ny, bgR, bfL, bwL);
-            to_prim_vjp(fL, wL, g, bwL, bfL);
-        }
-        const int flag = (usedL ? 1 : 0) | (usedR ? 2 : 0);  // the L / R face state is the linear reconstruction
-        aL[e] = bfL;
-        aR[e] = bfR;
-        aflag[e] = flag;
+    if (e >= m.E) return;
+    const int L = __ldg(&m.e_L[e]), R = __ldg(&m.e_R[e]);
+    const double* gm = &m.e_geom[(size_t)e * 8];
+    const double nx = __ldg(&gm[0]), ny = __ldg(&gm[1]), len = __ldg(&gm[2]);
+    const double mL = __ldg(&m.c_mvol[L]);
+    const d4 lL = ld4(&lam[L]);
+    d4 mu = mk4(mL * lL.x, mL * lL.y, mL * lL.z, mL * lL.w);
+    if (__ldg(&e_rlist[e])) {
+        const double mR = __ldg(&m.c_mvol[R]);
+        const d4 lR = ld4(&lam[R]);
+        mu = mk4(mu.x - mR * lR.x, mu.y - mR * lR.y, mu.z - mR * lR.z, mu.w - mR * lR.w);
     }
+    const size_t E = (size_t)tp.E;
+    const double* v = tp.v;
+    auto t = [&](int f) { return __ldg(&v[(size_t)f * E + e]); };
+    Prim wL{t(T_LR), t(T_LU), t(T_LV), t(T_LP), t(T_LIR)};
+    Prim wR{t(T_RR), t(T_RU), t(T_RV), t(T_RP), t(T_RIR)};
+    const d4 fL = mk4(wL.r, t(T_ULY), t(T_ULZ), t(T_ULW));
+    const d4 fR = mk4(wR.r, t(T_URY), t(T_URZ), t(T_URW));
+    RoeRec r;
+    r.ruL = t(T_RUL); r.ruR = t(T_RUR); r.HL = t(T_HL); r.HR = t(T_HR); r.irm = t(T_IRM); r.rm = t(T_RM);
+    r.rrorl = t(T_RRORL); r.w = t(T_W); r.um = t(T_UM); r.vm = t(T_VM); r.Hm = t(T_HM); r.am2 = t(T_AM2);
+    r.iam = t(T_IAM); r.am = t(T_AM); r.un = t(T_UN); r.sel = t(T_SEL); r.Mstar = t(T_MSTAR); r.dE = t(T_DE);
+    r.Etm = t(T_ETM); r.ae = t(T_AE); r.dUroe = t(T_DUROE); r.dProe = t(T_DPROE); r.dUr = t(T_DUR);
+    r.sub = (__ldg(&tp.flags[e]) & 4) != 0;
+    Prim bwL, bwR;
+    d4 bfL, bfR;
+    roe_rev(wL, wR, fL, fR, nx, ny, len, g, r, mu, bwL, bwR, bfL, bfR);
+    to_prim_vjp(fR, wR, g, bwR, bfR);
+    if (e >= m.E_int) {  // slip wall / symmetry: the ghost is a function of the L face state
+        ghost_slip_vjp(fL, wL, nx, ny, bfR, bfL, bwL);
+        bfR = mk4(0, 0, 0, 0);
+    }
+    to_prim_vjp(fL, wL, g, bwL, bfL);
+    aL[e] = bfL;
+    aR[e] = bfR;
 }
 
 // ---- per cell: gather face-state adjoints, then limiter + LSQ VJP ---------------
@@ -378,13 +367,14 @@ struct Adjoint {
     std::vector<d4*> chk;          // U at the start of each segment
     double* d_chk_t = nullptr;     // t at the start of each segment
     std::vector<d4*> seg_states;   // per step of a segment: U_0, U_1, U_2
-    std::vector<d4*> seg_gx, seg_gy;  // per stage of a segment's steps: the limited gradients
     std::vector<d4*> seg_R;           // per stage of a segment's steps: the residual R(U_in)
+    std::vector<double*> seg_tape;    // per stage of a segment's steps: the edge tape (kTapeFields x E)
+    std::vector<int*> seg_tflags;
     double* d_seg_dt = nullptr;    // per step: dt, dt_raw
     int* d_seg_cstar = nullptr;    // per step: the minimising cell
     d4 *d_lam = nullptr, *d_lam_in = nullptr, *d_acc0 = nullptr, *d_aL = nullptr, *d_aR = nullptr;
     d4 *d_lamdir = nullptr, *d_bdU = nullptr, *d_keepU = nullptr;
-    int *d_aflag = nullptr, *d_rlist = nullptr, *d_rev = nullptr;
+    int *d_rlist = nullptr, *d_rev = nullptr;
     double* d_dotp = nullptr;
     bool ready = false;
     bool last_kept = false;  // the segment buffers hold the last segment's steps
@@ -448,18 +438,17 @@ struct Adjoint {
         seg_states.assign((size_t)S * nst, nullptr);
         for (auto& q : seg_states)
             if ((rc = alloc(q, N))) return rc;
-        const bool linear = p.reconstruct == 3002;
-        seg_gx.assign(linear ? (size_t)S * nst : 0, nullptr);
-        seg_gy.assign(seg_gx.size(), nullptr);
-        for (size_t i = 0; i < seg_gx.size(); i++)
-            if ((rc = alloc(seg_gx[i], N)) || (rc = alloc(seg_gy[i], N))) return rc;
         seg_R.assign((size_t)S * nst, nullptr);
         for (auto& q : seg_R)
             if ((rc = alloc(q, N))) return rc;
+        seg_tape.assign((size_t)S * nst, nullptr);
+        seg_tflags.assign((size_t)S * nst, nullptr);
+        for (size_t i = 0; i < seg_tape.size(); i++)
+            if ((rc = alloc(seg_tape[i], (size_t)dev::kTapeFields * E)) || (rc = alloc(seg_tflags[i], E))) return rc;
         const int nb = nblk(N, 256);
         if ((rc = alloc(d_seg_dt, 2 * (size_t)S)) || (rc = alloc(d_seg_cstar, S)) || (rc = alloc(d_lam, N)) ||
             (rc = alloc(d_lam_in, N)) || (rc = alloc(d_acc0, N)) || (rc = alloc(d_aL, E)) || (rc = alloc(d_aR, E)) ||
-            (rc = alloc(d_lamdir, N)) || (rc = alloc(d_keepU, N)) || (rc = alloc(d_bdU, 3 * (size_t)N)) || (rc = alloc(d_aflag, E)) ||
+            (rc = alloc(d_lamdir, N)) || (rc = alloc(d_keepU, N)) || (rc = alloc(d_bdU, 3 * (size_t)N)) ||
             (rc = alloc(d_dotp, (size_t)nb * 3)))
             return rc;
         return 0;
@@ -481,14 +470,12 @@ struct Adjoint {
         dev::launch_dt_final(st, v.d_state, true);
         AK(cudaMemcpyAsync(d_seg_dt + 2 * slot, &v.d_state->dt, sizeof(double), cudaMemcpyDeviceToDevice, st));
         AK(cudaMemcpyAsync(d_seg_dt + 2 * slot + 1, &v.d_state->dt_raw, sizeof(double), cudaMemcpyDeviceToDevice, st));
-        // each stage's gradients go to the segment's buffers (kept for the reverse sweep)
-        d4 *gx0 = v.d_Gx, *gy0 = v.d_Gy;
+        // each stage's residual and edge tape go to the segment's buffers (kept for the reverse sweep)
         auto stage = [&](int si, int kind) {
-            if (!seg_gx.empty()) {
-                v.d_Gx = seg_gx[(size_t)slot * nst + si];
-                v.d_Gy = seg_gy[(size_t)slot * nst + si];
-            }
             v.d_rec_R = seg_R[(size_t)slot * nst + si];
+            v.rec_tape.v = seg_tape[(size_t)slot * nst + si];
+            v.rec_tape.flags = seg_tflags[(size_t)slot * nst + si];
+            v.rec_tape.E = v.E;
             v.enqueue_stage(kind);
         };
         if (v.p.time_advance == 3101) {
@@ -500,9 +487,8 @@ struct Adjoint {
             AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst + 2], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
             stage(2, dev::STAGE_SSP_3);
         }
-        v.d_Gx = gx0;
-        v.d_Gy = gy0;
         v.d_rec_R = nullptr;
+        v.rec_tape = dev::EdgeTape();
         dev::launch_restrict(st, v.d_U, v.mv, v.d_cell_ref, v.d_cell_new, v.d_flags, v.d_flag_count, Solver::kFlagCap,
                              v.p.restrict_ref, v.gas, v.d_status);
         AK(cudaGetLastError());
@@ -511,23 +497,19 @@ struct Adjoint {
 
     // one stage VJP: lam_s (d_lam) -> lam_in (d_lam_in), acc0, partial F.mu in dot slot;
     // (Uin, Gx, Gy): the stage's input state and the limited gradients the forward used
-    int stage_vjp(const d4* Uin, const d4* Gx, const d4* Gy, const d4* Rs, const double* dt_p, double a, double b,
+    int stage_vjp(const d4* Uin, const dev::EdgeTape& tape, const d4* Rs, const double* dt_p, double a, double b,
                   int acc_mode, int dot_slot) {
         Solver& v = *s;
         cudaStream_t st = v.stream;
         const bool linear = v.p.reconstruct == 3002;
         const int nbE = nblk(v.E, dev::kEdgeThreads), nbN = nblk(v.N, 256);
         double* dp = d_dotp + (size_t)dot_slot * nbN;
-        if (linear)
-            dev::k_adj_edge<true><<<nbE, dev::kEdgeThreads, 0, st>>>(Uin, Gx, Gy, v.mv, v.gas, d_lam, d_rlist, d_aL,
-                                                                     d_aR, d_aflag);
-        else
-            dev::k_adj_edge<false><<<nbE, dev::kEdgeThreads, 0, st>>>(Uin, Gx, Gy, v.mv, v.gas, d_lam, d_rlist, d_aL,
-                                                                      d_aR, d_aflag);
-        if (!linear) dev::k_adj_cell<false, false><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, d_aflag, d_lamdir, d_bdU);
+        dev::k_adj_edge<<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, d_lam, d_rlist, d_aL, d_aR);
+        const int* fl = tape.flags;
+        if (!linear) dev::k_adj_cell<false, false><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, fl, d_lamdir, d_bdU);
         else if (v.p.limiter == 1)
-            dev::k_adj_cell<true, true><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, d_aflag, d_lamdir, d_bdU);
-        else dev::k_adj_cell<true, false><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, d_aflag, d_lamdir, d_bdU);
+            dev::k_adj_cell<true, true><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, fl, d_lamdir, d_bdU);
+        else dev::k_adj_cell<true, false><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, fl, d_lamdir, d_bdU);
         dev::k_adj_combine<<<nbN, 256, 0, st>>>(v.mv, d_rev, d_lamdir, d_bdU, d_lam, Rs, dt_p, a, b, acc_mode,
                                                 d_lam_in, d_acc0, linear ? 1 : 0, dp);
         AK(cudaGetLastError());
@@ -541,26 +523,31 @@ struct Adjoint {
         const double* dtp = d_seg_dt + 2 * slot;
         const int nbN = nblk(v.N, 256);
         auto R = [&](int si) { return seg_R[(size_t)slot * nst + si]; };
-        auto gx = [&](int si) { return seg_gx.empty() ? v.d_Gx : seg_gx[(size_t)slot * nst + si]; };
-        auto gy = [&](int si) { return seg_gy.empty() ? v.d_Gy : seg_gy[(size_t)slot * nst + si]; };
+        auto tp = [&](int si) {
+            dev::EdgeTape t;
+            t.v = seg_tape[(size_t)slot * nst + si];
+            t.flags = seg_tflags[(size_t)slot * nst + si];
+            t.E = v.E;
+            return t;
+        };
         int rc;
         double b0 = 1.0, b1 = 0.0, b2 = 0.0;  // b_s of the stages in reverse order
         if (v.p.time_advance == 3101) {
             // U1 = U0 + dt R(U0): a = 0, b = 1
-            if ((rc = stage_vjp(seg_states[(size_t)slot], gx(0), gy(0), R(0), dtp, 0.0, 1.0, 2, 0))) return rc;
+            if ((rc = stage_vjp(seg_states[(size_t)slot], tp(0), R(0), dtp, 0.0, 1.0, 2, 0))) return rc;
             std::swap(d_lam, d_lam_in);
         } else {
             const d4* U0 = seg_states[(size_t)slot * 3];
             const d4* U1 = seg_states[(size_t)slot * 3 + 1];
             const d4* U2 = seg_states[(size_t)slot * 3 + 2];
             // U3 = 1/3 U0 + 2/3 (U2 + dt R(U2))
-            if ((rc = stage_vjp(U2, gx(2), gy(2), R(2), dtp, 1.0 / 3.0, 2.0 / 3.0, 0, 0))) return rc;
+            if ((rc = stage_vjp(U2, tp(2), R(2), dtp, 1.0 / 3.0, 2.0 / 3.0, 0, 0))) return rc;
             std::swap(d_lam, d_lam_in);
             // U2 = 3/4 U0 + 1/4 (U1 + dt R(U1))
-            if ((rc = stage_vjp(U1, gx(1), gy(1), R(1), dtp, 0.75, 0.25, 1, 1))) return rc;
+            if ((rc = stage_vjp(U1, tp(1), R(1), dtp, 0.75, 0.25, 1, 1))) return rc;
             std::swap(d_lam, d_lam_in);
             // U1 = U0 + dt R(U0); U0 also feeds stages 2 and 3 directly (acc0)
-            if ((rc = stage_vjp(U0, gx(0), gy(0), R(0), dtp, 0.0, 1.0, 3, 2))) return rc;
+            if ((rc = stage_vjp(U0, tp(0), R(0), dtp, 0.0, 1.0, 3, 2))) return rc;
             std::swap(d_lam, d_lam_in);
             b0 = 2.0 / 3.0;
             b1 = 0.25;

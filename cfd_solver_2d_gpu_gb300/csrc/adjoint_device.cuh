@@ -27,120 +27,117 @@ __device__ __forceinline__ void to_prim_vjp(const d4 U, const Prim& w, const Gas
     bU.x += bw.r + bw.p * g.ga1 * q - b_ir * w.ir * w.ir;
 }
 
-// adjoint of roe_flux (physics.cuh): bF -> adjoints of the two primitive states
-__device__ __forceinline__ void roe_flux_vjp(const Prim& L, const Prim& R, double nx, double ny, double area,
-                                             const Gas& g, const d4 bF, Prim& bL, Prim& bR) {
-    // ---- forward, exactly as roe_flux ----
-    const double unL = nx * L.u + ny * L.v, unR = nx * R.u + ny * R.v;
-    const double ruL = L.r * unL, ruR = R.r * unR;
-    const double V2L = L.u * L.u + L.v * L.v, V2R = R.u * R.u + R.v * R.v;
-    const double EL = L.p * L.ir, ER = R.p * R.ir;
-    const double HL = fma(g.gam_over_ga1, EL, 0.5 * V2L);
-    const double HR = fma(g.gam_over_ga1, ER, 0.5 * V2R);
+// adjoint of roe_flux (physics.cuh): bF -> adjoints of the two primitive states (bL, bR,
+// including 1/rho in .ir) and of the conserved face states the flux reads directly
+// (bUL, bUR: the momenta through the mass flux, rho E through H and dE); all four are
+// overwritten.  r holds the forward's intermediates (roe_core<true>); the few cheap ones
+// not kept are recomputed with roe_core's operations, and the reverse follows the
+// forward backwards through the factorisations roe_core uses.
+__device__ __forceinline__ void roe_rev(const Prim& L, const Prim& R, const d4 UL, const d4 UR, double nx, double ny,
+                                        double area, const Gas& g, const RoeRec& r, const d4 bF, Prim& bL, Prim& bR,
+                                        d4& bUL, d4& bUR) {
+    const double ruL = r.ruL, ruR = r.ruR, HL = r.HL, HR = r.HR, irm = r.irm, rm = r.rm, rrorl = r.rrorl, w = r.w;
+    const double um = r.um, vm = r.vm, Hm = r.Hm, am2 = r.am2, iam = r.iam, am = r.am, un = r.un, sel = r.sel;
+    const double Mstar = r.Mstar, dE = r.dE, Etm = r.Etm, ae = r.ae, dUroe = r.dUroe, dProe = r.dProe, dUr = r.dUr;
+    const bool sub = r.sub;
+    const double sL = UL.w + L.p, sR = UR.w + R.p;
     const double prod = R.r * L.r;
-    const double irm = rsqrt(prod);
-    const double rm = prod * irm;
-    const double rrorl = R.r * irm;
-    const double w = rcp(rrorl + 1.0);
     const double Xu = fma(R.u, rrorl, L.u), Xv = fma(R.v, rrorl, L.v), XH = fma(HR, rrorl, HL);
-    const double um = Xu * w, vm = Xv * w, Hm = XH * w;
-    const double Vm2 = um * um + vm * vm;
-    const double am2 = g.ga1 * (Hm - 0.5 * Vm2);
-    const double iam = rsqrt(am2);
-    const double am = am2 * iam;
-    const double un = um * nx + vm * ny;
-    const double eig1 = fabs(un), eig2 = fabs(un + am), eig3 = fabs(un - am);
-    const double dE = (HR - ER) - (HL - EL);
-    const double Etm = fma(g.Etm_c, Vm2, Hm * g.inv_gamma);
+    const double eig1 = fabs(un);
     const double dW0 = R.r - L.r;
     const double du = R.u - L.u, dv = R.v - L.v;
     const double dW1 = fma(rm, du, dW0 * um);
     const double dW2 = fma(rm, dv, dW0 * vm);
     const double dW3 = fma(rm, dE, dW0 * Etm);
-    const double Mstar = (eig2 - eig3) * 0.5 * iam;
     const double dun = fma(nx, du, ny * dv);
     const double dp = R.p - L.p;
-    const double astar = (eig2 + eig3) * 0.5;
-    const double ae = astar - eig1;
     const double iam2 = iam * iam;
-    const double dUroe = fma(Mstar, dun, ae * dp * irm * iam2);
-    const double dProe = fma(Mstar, dp, ae * rm * dun);
-    const double dUr = dUroe * rm;
+    const double t1 = ae * dp, t12 = t1 * irm;   // dUroe's second term is t12 iam2
+    const double t3 = ae * rm;                   // dProe's second term is t3 dun
     const double h = 0.5 * area;
     // ---- reverse ----
     const double bC0 = h * bF.x, bC1 = h * bF.y, bC2 = h * bF.z, bC3 = h * bF.w;  // central part
     const double bD0 = -bC0, bD1 = -bC1, bD2 = -bC2, bD3 = -bC3;                   // dissipation
     double b_eig1 = bD0 * dW0 + bD1 * dW1 + bD2 * dW2 + bD3 * dW3;
-    double b_dW0 = bD0 * eig1, b_dW1 = bD1 * eig1, b_dW2 = bD2 * eig1, b_dW3 = bD3 * eig1;
+    double b_dW0 = bD0 * eig1;
+    const double b_dW1 = bD1 * eig1, b_dW2 = bD2 * eig1, b_dW3 = bD3 * eig1;
     const double b_dUr = bD0 + bD1 * um + bD2 * vm + bD3 * Hm;
     double b_um = bD1 * dUr, b_vm = bD2 * dUr, b_Hm = bD3 * dUr;
     const double b_dProe = bD1 * nx + bD2 * ny + bD3 * un;
     double b_un = bD3 * dProe;
+    // dUr = dUroe rm
     const double b_dUroe = b_dUr * rm;
     double b_rm = b_dUr * dUroe;
+    // dProe = Mstar dp + t3 dun
     double b_Mstar = b_dProe * dp;
     double b_dp = b_dProe * Mstar;
-    double b_ae = b_dProe * rm * dun;
-    b_rm += b_dProe * ae * dun;
-    double b_dun = b_dProe * ae * rm;
+    const double b_t3 = b_dProe * dun;
+    double b_dun = b_dProe * t3;
+    double b_ae = b_t3 * rm;
+    b_rm += b_t3 * ae;
+    // dUroe = Mstar dun + t12 iam2
     b_Mstar += b_dUroe * dun;
     b_dun += b_dUroe * Mstar;
-    b_ae += b_dUroe * dp * irm * iam2;
-    b_dp += b_dUroe * ae * irm * iam2;
-    double b_irm = b_dUroe * ae * dp * iam2;
-    double b_iam = b_dUroe * ae * dp * irm * 2.0 * iam;
-    const double b_astar = b_ae;
-    b_eig1 -= b_ae;
+    const double b_iam2 = b_dUroe * t12;
+    const double b_t12 = b_dUroe * iam2;
+    double b_irm = b_t12 * t1;
+    const double b_t1 = b_t12 * irm;
+    b_ae += b_t1 * dp;
+    b_dp += b_t1 * ae;
+    double b_iam = 2.0 * iam * b_iam2;
+    // ae = astar - eig1; astar = am or eig1
+    double b_am = sub ? b_ae : 0.0;
+    b_eig1 += sub ? -b_ae : 0.0;  // astar = eig1 when not sub: the two cancel
+    // dp, dun, dW*, dE, Etm
     double b_Rp = b_dp, b_Lp = -b_dp;
     double b_du = b_dun * nx, b_dv = b_dun * ny;
-    double b_eig2 = b_Mstar * 0.5 * iam, b_eig3 = -b_Mstar * 0.5 * iam;
-    b_iam += b_Mstar * (eig2 - eig3) * 0.5;
-    b_eig2 += 0.5 * b_astar;
-    b_eig3 += 0.5 * b_astar;
-    b_rm += b_dW3 * dE;
+    b_rm += b_dW3 * dE + b_dW2 * dv + b_dW1 * du;
     const double b_dE = b_dW3 * rm;
-    b_dW0 += b_dW3 * Etm;
     const double b_Etm = b_dW3 * dW0;
-    b_rm += b_dW2 * dv;
+    b_dW0 += b_dW3 * Etm + b_dW2 * vm + b_dW1 * um;
     b_dv += b_dW2 * rm;
-    b_dW0 += b_dW2 * vm;
     b_vm += b_dW2 * dW0;
-    b_rm += b_dW1 * du;
     b_du += b_dW1 * rm;
-    b_dW0 += b_dW1 * um;
     b_um += b_dW1 * dW0;
-    double b_Ru = b_du, b_Lu = -b_du, b_Rv = b_dv, b_Lv = -b_dv;
     double b_Rr = b_dW0, b_Lr = -b_dW0;
+    double b_Ru = b_du, b_Lu = -b_du, b_Rv = b_dv, b_Lv = -b_dv;
     double b_Vm2 = b_Etm * g.Etm_c;
     b_Hm += b_Etm * g.inv_gamma;
-    double b_HR = b_dE, b_ER = -b_dE, b_HL = -b_dE, b_EL = b_dE;
+    // dE = URw Rir - ULw Lir
+    double b_URw = b_dE * R.ir, b_ULw = -b_dE * L.ir;
+    double b_Rir = b_dE * UR.w, b_Lir = -b_dE * UL.w;
+    // Mstar = sel iam; sel = un (sub) or copysign(am, un)
+    const double b_sel = b_Mstar * iam;
+    b_iam += b_Mstar * sel;
+    if (sub) b_un += b_sel;
+    else b_am += b_sel * copysign(1.0, un);
+    // eig1 = |un|; un = um nx + vm ny
     b_un += b_eig1 * sgn(un);
-    const double s2 = sgn(un + am), s3 = sgn(un - am);
-    b_un += b_eig2 * s2 + b_eig3 * s3;
-    const double b_am = b_eig2 * s2 - b_eig3 * s3;
     b_um += b_un * nx;
     b_vm += b_un * ny;
+    // am = am2 iam; iam = am2^(-1/2); am2 = ga1 (Hm - Vm2/2); Vm2 = um^2 + vm^2
     double b_am2 = b_am * iam;
     b_iam += b_am * am2;
-    b_am2 += b_iam * (-0.5 * iam * iam2);
+    b_am2 -= 0.5 * b_iam * iam * iam2;
     b_Hm += b_am2 * g.ga1;
-    b_Vm2 += -0.5 * g.ga1 * b_am2;
+    b_Vm2 -= 0.5 * g.ga1 * b_am2;
     b_um += 2.0 * um * b_Vm2;
     b_vm += 2.0 * vm * b_Vm2;
+    // (um, vm, Hm) = (Xu, Xv, XH) w
     const double b_w = b_um * Xu + b_vm * Xv + b_Hm * XH;
     const double bXu = b_um * w, bXv = b_vm * w, bXH = b_Hm * w;
     b_Ru += bXu * rrorl;
     b_Lu += bXu;
     b_Rv += bXv * rrorl;
     b_Lv += bXv;
-    b_HR += bXH * rrorl;
-    b_HL += bXH;
+    double b_HR = bXH * rrorl, b_HL = bXH;
     double b_rrorl = bXu * R.u + bXv * R.v + bXH * HR - b_w * w * w;
+    // rrorl = Rr irm; rm = prod irm; irm = prod^(-1/2); prod = Rr Lr
     b_Rr += b_rrorl * irm;
     b_irm += b_rrorl * R.r;
     double b_prod = b_rm * irm;
     b_irm += b_rm * prod;
-    b_prod += b_irm * (-0.5 * irm * irm * irm);
+    b_prod -= 0.5 * b_irm * irm * irm * irm;
     b_Rr += b_prod * L.r;
     b_Lr += b_prod * R.r;
     // central flux (ruL + ruR, ruL uL + ruR uR + nx psum, ruL vL + ruR vR + ny psum, ruL HL + ruR HR)
@@ -155,44 +152,27 @@ __device__ __forceinline__ void roe_flux_vjp(const Prim& L, const Prim& R, doubl
     const double b_psum = bC1 * nx + bC2 * ny;
     b_Lp += b_psum;
     b_Rp += b_psum;
-    b_EL += b_HL * g.gam_over_ga1;
-    b_ER += b_HR * g.gam_over_ga1;
-    const double b_V2L = 0.5 * b_HL, b_V2R = 0.5 * b_HR;
-    b_Lp += b_EL * L.ir;
-    b_Rp += b_ER * R.ir;
-    const double b_Lir = b_EL * L.p, b_Rir = b_ER * R.p;
-    b_Lu += 2.0 * L.u * b_V2L;
-    b_Lv += 2.0 * L.v * b_V2L;
-    b_Ru += 2.0 * R.u * b_V2R;
-    b_Rv += 2.0 * R.v * b_V2R;
-    b_Lr += b_ruL * unL;
-    b_Rr += b_ruR * unR;
-    const double b_unL = b_ruL * L.r, b_unR = b_ruR * R.r;
-    b_Lu += b_unL * nx;
-    b_Lv += b_unL * ny;
-    b_Ru += b_unR * nx;
-    b_Rv += b_unR * ny;
+    // H = (rho E + p) / rho
+    b_ULw += b_HL * L.ir;
+    b_Lp += b_HL * L.ir;
+    b_Lir += b_HL * sL;
+    b_URw += b_HR * R.ir;
+    b_Rp += b_HR * R.ir;
+    b_Rir += b_HR * sR;
     bL.r = b_Lr; bL.u = b_Lu; bL.v = b_Lv; bL.p = b_Lp; bL.ir = b_Lir;
     bR.r = b_Rr; bR.u = b_Ru; bR.v = b_Rv; bR.p = b_Rp; bR.ir = b_Rir;
+    // mass fluxes n . (rho u)
+    bUL = mk4(0.0, b_ruL * nx, b_ruL * ny, b_ULw);
+    bUR = mk4(0.0, b_ruR * nx, b_ruR * ny, b_URw);
 }
 
-// face_state (step_device.cuh) that also reports whether the linear reconstruction was kept
-template <bool LINEAR>
-__device__ __forceinline__ d4 face_state_used(const d4 u, const d4 gx, const d4 gy, double dx, double dy,
-                                              const Gas& g, Prim& w, bool& used) {
-    used = false;
-    if (!LINEAR) {
-        w = to_prim(u, g);
-        return u;
-    }
-    const d4 f = lin(u, gx, gy, dx, dy);
-    w = to_prim(f, g);
-    if (out_of_range(w.r, w.p)) {
-        w = to_prim(u, g);
-        return u;
-    }
-    used = true;
-    return f;
+// the same with the forward recomputed (for a caller without the recorded intermediates)
+__device__ __forceinline__ void roe_flux_vjp(const Prim& L, const Prim& R, const d4 UL, const d4 UR, double nx,
+                                             double ny, double area, const Gas& g, const d4 bF, Prim& bL, Prim& bR,
+                                             d4& bUL, d4& bUR) {
+    RoeRec r;
+    roe_core<true>(L, R, UL, UR, nx, ny, area, g, &r);
+    roe_rev(L, R, UL, UR, nx, ny, area, g, r, bF, bL, bR, bUL, bUR);
 }
 
 // adjoint of ghost_slip (physics.cuh): bUR -> bUL (ghost_slip reads UL.x, UL.w and the

@@ -106,15 +106,25 @@ __device__ __forceinline__ d4 lin(const d4 U, const d4 gx, const d4 gy, double d
                         fma(gy.z, dy, fma(gx.z, dx, U.z)), fma(gy.w, dy, fma(gx.w, dx, U.w)));
 }
 
+// The forward values the Roe flux's reverse (roe_rev, adjoint_device.cuh) reads, kept
+// per edge by the recorded forward of the discrete adjoint so that the reverse sweep
+// need not recompute them (memory is cheap next to FP64 issue on this part).
+struct RoeRec {
+    double ruL, ruR, HL, HR, irm, rm, rrorl, w, um, vm, Hm, am2, iam, am, un, sel, Mstar, dE, Etm, ae, dUroe,
+        dProe, dUr;
+    bool sub;
+};
+
 // ConvectRoeCommon2d + RoeDissapationTerm2d, FVMR/src/space/convection/Roe.cpp:380-538
 // (entropy fix off, static mesh).  L, R: the face states' primitive variables; UL, UR
 // the same states conserved.  Exact identities save FP64 work: the mass flux is
 // n . (rho u) from the momentum, the total enthalpy H = gamma/(gamma-1) p/rho + V^2/2
 // is (rho E + p)/rho, H - p/rho is rho E/rho, and with a > 0
 // (|un + a| + |un - a|)/2 = max(|un|, a), (|un + a| - |un - a|)/2 = un if |un| < a,
-// else a sgn(un).
-__device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, const d4 UL, const d4 UR, double nx, double ny,
-                                       double area, const Gas& g) {
+// else a sgn(un).  With REC the intermediates also go to *rec.
+template <bool REC>
+__device__ __forceinline__ d4 roe_core(const Prim& L, const Prim& R, const d4 UL, const d4 UR, double nx, double ny,
+                                       double area, const Gas& g, RoeRec* rec) {
     const double ruL = fma(nx, UL.y, ny * UL.z), ruR = fma(nx, UR.y, ny * UR.z);
     const double HL = (UL.w + L.p) * L.ir, HR = (UR.w + R.p) * R.ir;
     const double psum = L.p + R.p;
@@ -136,9 +146,11 @@ __device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, const d4 UL
     const double am = am2 * iam;
     const double un = fma(um, nx, vm * ny);
     const double eig1 = fabs(un);
-    const double astar = dmax(eig1, am);                                   // (eig2 + eig3) / 2
-    const double Mstar = (dlt(eig1, am) ? un : copysign(am, un)) * iam;   // (eig2 - eig3) / (2 am)
-    const double dE = fma(UR.w, R.ir, -UL.w * L.ir);                        // (HR - ER) - (HL - EL)
+    const bool sub = dlt(eig1, am);                      // |un| < am
+    const double astar = sub ? am : eig1;                // (eig2 + eig3) / 2 = dmax(eig1, am)
+    const double sel = sub ? un : copysign(am, un);
+    const double Mstar = sel * iam;                      // (eig2 - eig3) / (2 am)
+    const double dE = fma(UR.w, R.ir, -UL.w * L.ir);   // (HR - ER) - (HL - EL)
     const double Etm = fma(g.Etm_c, Vm2, Hm * g.inv_gamma);
     const double dW0 = R.r - L.r;
     const double du = R.u - L.u, dv = R.v - L.v;
@@ -156,7 +168,18 @@ __device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, const d4 UL
     F.y = h * (F.y - fma(eig1, dW1, fma(dUr, um, dProe * nx)));
     F.z = h * (F.z - fma(eig1, dW2, fma(dUr, vm, dProe * ny)));
     F.w = h * (F.w - fma(eig1, dW3, fma(dUr, Hm, dProe * un)));
+    if (REC) {
+        rec->ruL = ruL; rec->ruR = ruR; rec->HL = HL; rec->HR = HR; rec->irm = irm; rec->rm = rm;
+        rec->rrorl = rrorl; rec->w = w; rec->um = um; rec->vm = vm; rec->Hm = Hm; rec->am2 = am2; rec->iam = iam;
+        rec->am = am; rec->un = un; rec->sel = sel; rec->Mstar = Mstar; rec->dE = dE; rec->Etm = Etm; rec->ae = ae;
+        rec->dUroe = dUroe; rec->dProe = dProe; rec->dUr = dUr; rec->sub = sub;
+    }
     return F;
+}
+
+__device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, const d4 UL, const d4 UR, double nx, double ny,
+                                       double area, const Gas& g) {
+    return roe_core<false>(L, R, UL, UR, nx, ny, area, g, nullptr);
 }
 
 // LocalLaxFriedrichs, FVMR/src/space/convection/LocalLaxFriedrichs.cpp:4-47

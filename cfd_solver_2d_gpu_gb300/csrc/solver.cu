@@ -224,7 +224,7 @@ void Solver::enqueue_stage(int kind) {
     }
     mark(PROF_FLUX, true);
     dev::launch_flux(s, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv, gas, bc, d_F,
-                     d_status);
+                     d_status, rec_tape.v ? &rec_tape : nullptr);
     mark(PROF_FLUX, false);
     launches += (mv.E_int > 0) + (mv.E > mv.E_int);
     mark(PROF_UPDATE, true);

@@ -211,11 +211,59 @@ __device__ __forceinline__ d4 face_state(const d4 u, const d4 gx, const d4 gy, d
     return f;
 }
 
-// an interior or periodic edge (R reconstructed at the partner's midpoint for periodic ones)
-template <int FLUX, bool LINEAR, bool NS>
+// face_state that also reports whether the linear reconstruction was kept
+template <bool LINEAR>
+__device__ __forceinline__ d4 face_state_used(const d4 u, const d4 gx, const d4 gy, double dx, double dy,
+                                              const Gas& g, Prim& w, bool& used) {
+    used = false;
+    if (!LINEAR) {
+        w = to_prim(u, g);
+        return u;
+    }
+    const d4 f = lin(u, gx, gy, dx, dy);
+    w = to_prim(f, g);
+    if (out_of_range(w.r, w.p)) {
+        w = to_prim(u, g);
+        return u;
+    }
+    used = true;
+    return f;
+}
+
+// ---- the discrete adjoint's tape of one stage's Roe edge fluxes (Euler equations):
+// per edge the two face states (primitive and conserved), the Roe flux's intermediates
+// (RoeRec) and a flag word (bit 0 / 1: the L / R face state is the linear
+// reconstruction; bit 2: |un| < am), field-major so that each field is one coalesced row
+enum TapeField : int {
+    T_LR, T_LU, T_LV, T_LP, T_LIR, T_RR, T_RU, T_RV, T_RP, T_RIR, T_ULY, T_ULZ, T_ULW, T_URY, T_URZ, T_URW,
+    T_RUL, T_RUR, T_HL, T_HR, T_IRM, T_RM, T_RRORL, T_W, T_UM, T_VM, T_HM, T_AM2, T_IAM, T_AM, T_UN, T_SEL,
+    T_MSTAR, T_DE, T_ETM, T_AE, T_DUROE, T_DPROE, T_DUR, kTapeFields
+};
+struct EdgeTape {
+    double* v = nullptr;   // [kTapeFields][E]
+    int* flags = nullptr;  // [E]
+    int E = 0;
+};
+
+__device__ __forceinline__ void tape_put(const EdgeTape& t, int e, const Prim& L, const Prim& R, const d4 UL,
+                                         const d4 UR, const RoeRec& r, int flags) {
+    const size_t E = (size_t)t.E;
+    double* v = t.v;
+    const double vals[kTapeFields] = {L.r,    L.u,   L.v,     L.p,   L.ir,    R.r,    R.u,   R.v,     R.p,    R.ir,
+                                      UL.y,   UL.z,  UL.w,    UR.y,  UR.z,    UR.w,   r.ruL, r.ruR,   r.HL,   r.HR,
+                                      r.irm,  r.rm,  r.rrorl, r.w,   r.um,    r.vm,   r.Hm,  r.am2,   r.iam,  r.am,
+                                      r.un,   r.sel, r.Mstar, r.dE,  r.Etm,   r.ae,   r.dUroe, r.dProe, r.dUr};
+#pragma unroll
+    for (int f = 0; f < kTapeFields; f++) v[(size_t)f * E + e] = vals[f];
+    t.flags[e] = flags | (r.sub ? 4 : 0);
+}
+
+// an interior or periodic edge (R reconstructed at the partner's midpoint for periodic ones);
+// with REC (Roe, Euler) the edge's tape entry is written as well
+template <int FLUX, bool LINEAR, bool NS, bool REC = false>
 __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, const d4* __restrict__ Gx,
                                               const d4* __restrict__ Gy, const MeshView& m, const Gas& g,
-                                              d4* __restrict__ F) {
+                                              d4* __restrict__ F, EdgeTape tape = EdgeTape()) {
     const int L = __ldg(&m.e_L[e]), R = __ldg(&m.e_R[e]);
     const double2* gm = reinterpret_cast<const double2*>(&m.e_geom[(size_t)e * 8]);
     const double2 n01 = __ldg(&gm[0]), l23 = __ldg(&gm[1]);
@@ -230,6 +278,21 @@ __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, c
     }
     Prim wL, wR;
     d4 fL, fR;
+    if constexpr (REC) {
+        static_assert(!REC || (FLUX == FLUX_ROE && !NS), "the adjoint's tape covers the Roe flux of the Euler equations");
+        bool usedL = false, usedR = false;
+        double dLx = 0, dLy = 0, dRx = 0, dRy = 0;
+        if (LINEAR) {
+            const double2 dL = __ldg(&gm[2]), dR = __ldg(&gm[3]);
+            dLx = dL.x; dLy = dL.y; dRx = dR.x; dRy = dR.y;
+        }
+        fL = face_state_used<LINEAR>(uL, gxL, gyL, dLx, dLy, g, wL, usedL);
+        fR = face_state_used<LINEAR>(uR, gxR, gyR, dRx, dRy, g, wR, usedR);
+        RoeRec r;
+        F[e] = roe_core<true>(wL, wR, fL, fR, nx, ny, len, g, &r);
+        tape_put(tape, e, wL, wR, fL, fR, r, (usedL ? 1 : 0) | (usedR ? 2 : 0));
+        return;
+    }
     if (LINEAR) {
         const double2 dL = __ldg(&gm[2]), dR = __ldg(&gm[3]);
         fL = face_state<true>(uL, gxL, gyL, dL.x, dL.y, g, wL);
@@ -249,11 +312,13 @@ __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, c
     F[e] = flux;
 }
 
-// a boundary edge with a ghost state (walls, far field, inlet, outlet, symmetry)
-template <int FLUX, bool LINEAR, bool NS>
+// a boundary edge with a ghost state (walls, far field, inlet, outlet, symmetry); with REC
+// (Roe, Euler) the tape entry of slip-wall and symmetry edges is written as well
+template <int FLUX, bool LINEAR, bool NS, bool REC = false>
 __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, const d4* __restrict__ Gx,
                                               const d4* __restrict__ Gy, const MeshView& m, const Gas& g,
-                                              const BcData& bc, d4* __restrict__ F, Status* st) {
+                                              const BcData& bc, d4* __restrict__ F, Status* st,
+                                              EdgeTape tape = EdgeTape()) {
     const int L = __ldg(&m.e_L[e]);
     const int bt = __ldg(&m.e_bc[e]);
     const double* gm = &m.e_geom[(size_t)e * 8];
@@ -265,6 +330,19 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
         gyL = ld4(&Gy[L]);
     }
     Prim wL;
+    if constexpr (REC) {
+        if (bt == 6001 || bt == 6021) {
+        static_assert(!REC || (FLUX == FLUX_ROE && !NS), "the adjoint's tape covers the Roe flux of the Euler equations");
+        bool usedL = false;
+        const d4 fL = face_state_used<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL, usedL);
+        const d4 fR = ghost_slip(fL, wL, nx, ny);
+        const Prim wR = to_prim(fR, g);
+        RoeRec r;
+        F[e] = roe_core<true>(wL, wR, fL, fR, nx, ny, len, g, &r);
+        tape_put(tape, e, wL, wR, fL, fR, r, usedL ? 1 : 0);
+        return;
+        }
+    }
     const d4 fL = face_state<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL);
     d4 fR = mk4(0, 0, 0, 0);
     switch (bt) {

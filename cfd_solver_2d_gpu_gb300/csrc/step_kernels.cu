@@ -66,20 +66,20 @@ __global__ void __launch_bounds__(256) k_grad(const d4* __restrict__ U, MeshView
     if (c < m.N) grad_cell<GRAD, BARTH>(c, U, m, Gx, Gy);
 }
 
-template <int FLUX, bool LINEAR, bool NS>
+template <int FLUX, bool LINEAR, bool NS, bool REC>
 __global__ void __launch_bounds__(256) k_flux_interior(const d4* __restrict__ U, const d4* __restrict__ Gx,
                                                        const d4* __restrict__ Gy, MeshView m, Gas g,
-                                                       d4* __restrict__ F) {
+                                                       d4* __restrict__ F, EdgeTape tape) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < m.E_int) flux_interior<FLUX, LINEAR, NS>(e, U, Gx, Gy, m, g, F);
+    if (e < m.E_int) flux_interior<FLUX, LINEAR, NS, REC>(e, U, Gx, Gy, m, g, F, tape);
 }
 
-template <int FLUX, bool LINEAR, bool NS>
+template <int FLUX, bool LINEAR, bool NS, bool REC>
 __global__ void __launch_bounds__(128) k_flux_boundary(const d4* __restrict__ U, const d4* __restrict__ Gx,
                                                        const d4* __restrict__ Gy, MeshView m, Gas g, BcData bc,
-                                                       d4* __restrict__ F, Status* st) {
+                                                       d4* __restrict__ F, Status* st, EdgeTape tape) {
     const int e = m.E_int + blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < m.E) flux_boundary<FLUX, LINEAR, NS>(e, U, Gx, Gy, m, g, bc, F, st);
+    if (e < m.E) flux_boundary<FLUX, LINEAR, NS, REC>(e, U, Gx, Gy, m, g, bc, F, st, tape);
 }
 
 template <int KIND>
@@ -201,16 +201,24 @@ void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const Me
     }
 }
 
-template <int FLUX, bool LINEAR, bool NS>
+template <int FLUX, bool LINEAR, bool NS, bool REC = false>
 static void flux_impl(cudaStream_t s, const d4* U, const d4* Gx, const d4* Gy, const MeshView& m,
-                      const Gas& g, const BcData& bc, d4* F, Status* st) {
-    if (m.E_int > 0) k_flux_interior<FLUX, LINEAR, NS><<<blocks(m.E_int, 256), 256, 0, s>>>(U, Gx, Gy, m, g, F);
+                      const Gas& g, const BcData& bc, d4* F, Status* st, EdgeTape tape = EdgeTape()) {
+    if (m.E_int > 0)
+        k_flux_interior<FLUX, LINEAR, NS, REC><<<blocks(m.E_int, 256), 256, 0, s>>>(U, Gx, Gy, m, g, F, tape);
     if (m.E > m.E_int)
-        k_flux_boundary<FLUX, LINEAR, NS><<<blocks(m.E - m.E_int, 128), 128, 0, s>>>(U, Gx, Gy, m, g, bc, F, st);
+        k_flux_boundary<FLUX, LINEAR, NS, REC><<<blocks(m.E - m.E_int, 128), 128, 0, s>>>(U, Gx, Gy, m, g, bc, F, st,
+                                                                                          tape);
 }
 
 void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, const d4* Gx,
-                 const d4* Gy, const MeshView& m, const Gas& g, const BcData& bc, d4* F, Status* st) {
+                 const d4* Gy, const MeshView& m, const Gas& g, const BcData& bc, d4* F, Status* st,
+                 const EdgeTape* tape) {
+    if (tape && tape->v) {  // the adjoint's recorded forward: Roe, Euler equations only
+        if (linear) flux_impl<FLUX_ROE, true, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
+        else flux_impl<FLUX_ROE, false, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
+        return;
+    }
     if (scheme == FLUX_ROE) {
         if (linear) {
             if (ns) flux_impl<FLUX_ROE, true, true>(s, U, Gx, Gy, m, g, bc, F, st);

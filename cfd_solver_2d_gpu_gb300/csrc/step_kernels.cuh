@@ -20,7 +20,8 @@ void launch_dt(cudaStream_t s, const d4* prim, const MeshView& m, const Gas& g, 
 void launch_dt_final(cudaStream_t s, StepState* st, bool advance);
 void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const MeshView& m, d4* Gx, d4* Gy);
 void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, const d4* Gx,
-                 const d4* Gy, const MeshView& m, const Gas& g, const BcData& bc, d4* F, Status* st);
+                 const d4* Gy, const MeshView& m, const Gas& g, const BcData& bc, d4* F, Status* st,
+                 const EdgeTape* tape = nullptr);
 void launch_update(cudaStream_t s, int kind, d4* U, const d4* U0, d4* K1, d4* rhs,
                    const d4* F, const MeshView& m, const StepState* st, const Gas& g, int* flag_list,
                    unsigned int* flag_count, int flag_cap, Status* status, d4* rec_R = nullptr);
