@@ -11,8 +11,9 @@
 //
 // Memory: checkpoints of U every S = ceil(K / n_checkpoints) steps; during the
 // reverse sweep each segment is recomputed once, keeping per step U_0, U_1, U_2,
-// the stages' residuals and edge tapes, so the sweep costs one extra forward pass
-// and O(K/S N + S (6 N + 117 E)) doubles (sqrt(K) checkpoints: O(sqrt(K) N)).
+// the stages' residuals, edge tapes and limiter records, so the sweep costs one
+// extra forward pass and about K/S 4N + S (74 N + 117 E) doubles (sqrt(K)
+// checkpoints: O(sqrt(K) N)).
 //
 // Kernels of one stage VJP (all gathers, no atomics: deterministic):
 //   k_adj_edge     per edge: mu = seed-weighted flux adjoint, flux VJP from the stage's tape
@@ -20,9 +21,11 @@
 //   k_adj_combine  per cell: gather the neighbours' LSQ adjoints; the stage's RK combination;
 //                  block partials of lam_s . R_s (the time step's adjoint)
 // and once a step k_adj_dt.  The recorded forward keeps, per stage, the input state, the
-// residual R_s and the edge tape (face states and Roe intermediates, step_device.cuh), so
-// the reverse sweep recomputes none of them: on this part FP64 issue, not memory, is
-// scarce (39 doubles a stage per edge; 3.9 GB for 23 steps of the 256x256 mesh).
+// residual R_s, the edge tape (face states and Roe intermediates) and the limiter record
+// (gradient before the limiter, phi, 1/den, the limiting slot and vertex; step_device.cuh),
+// so the reverse sweep recomputes none of them: on this part FP64 issue, not memory, is
+// scarce (39 doubles a stage per edge and 16.5 per cell; 5 GB for 23 steps of the
+// 256x256 mesh).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -89,9 +92,11 @@ __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView
 }
 
 // ---- per cell: gather face-state adjoints, then limiter + LSQ VJP ---------------
+// The limiter's choices and the gradient before it come from the stage's record
+// (grad_cell<1, true, true>); nothing of the forward is recomputed.
 template <bool LINEAR, bool BARTH>
-__global__ void __launch_bounds__(256) k_adj_cell(const d4* __restrict__ U, MeshView m, const d4* __restrict__ aL,
-                                                  const d4* __restrict__ aR, const int* __restrict__ aflag,
+__global__ void __launch_bounds__(256) k_adj_cell(MeshView m, const d4* __restrict__ aL, const d4* __restrict__ aR,
+                                                  const int* __restrict__ aflag, CellTape ct,
                                                   d4* __restrict__ lam_dir, d4* __restrict__ bdU) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
@@ -107,6 +112,7 @@ __global__ void __launch_bounds__(256) k_adj_cell(const d4* __restrict__ U, Mesh
         const double* gm = &m.e_geom[(size_t)e * 8];
         const double dx = isL ? __ldg(&gm[4]) : __ldg(&gm[6]);
         const double dy = isL ? __ldg(&gm[5]) : __ldg(&gm[7]);
+#pragma unroll
         for (int v = 0; v < 4; v++) {
             lu[v] += av[v];
             if (LINEAR && used) {
@@ -118,77 +124,55 @@ __global__ void __launch_bounds__(256) k_adj_cell(const d4* __restrict__ U, Mesh
     lam_dir[c] = mk4(lu[0], lu[1], lu[2], lu[3]);
     double bd[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
     if (LINEAR) {
-        // recompute the raw gradient and the limiter's choices (grad_cell, least squares)
-        const d4 uc = ld4(&U[c]);
         const int nnb = __ldg(&m.c_nnb[c]);
-        const double ucv[4] = {uc.x, uc.y, uc.z, uc.w};
-        double dU[3][4];
-        for (int k = 0; k < 3; k++) {
-            const int q = __ldg(&m.c_nbr[c * 3 + k]);
-            const d4 un = (k < nnb) ? ld4(&U[q]) : uc;
-            const double unv[4] = {un.x, un.y, un.z, un.w};
-            for (int v = 0; v < 4; v++) dU[k][v] = unv[v] - ucv[v];
-        }
         const double* B = &m.c_lsq[(size_t)c * 6];
         double b0[3], b1[3];
+#pragma unroll
         for (int k = 0; k < 3; k++) {
             b0[k] = __ldg(&B[k]);
             b1[k] = __ldg(&B[3 + k]);
         }
-        const double* X = &m.c_vtx[(size_t)c * 6];
-        double vx[3], vy[3];
-        for (int j = 0; j < 3; j++) {
-            vx[j] = __ldg(&X[2 * j]);
-            vy[j] = __ldg(&X[2 * j + 1]);
+        double vx[3] = {0, 0, 0}, vy[3] = {0, 0, 0}, gxr[4] = {0, 0, 0, 0}, gyr[4] = {0, 0, 0, 0};
+        double phi[4] = {1, 1, 1, 1}, rden[4] = {0, 0, 0, 0};
+        int code = 0;
+        if (BARTH) {
+            const double* X = &m.c_vtx[(size_t)c * 6];
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                vx[j] = __ldg(&X[2 * j]);
+                vy[j] = __ldg(&X[2 * j + 1]);
+            }
+            code = __ldg(&ct.code[c]);
+            if (code) {
+                const d4 a = ld4(&ct.gx[c]), bb = ld4(&ct.gy[c]), p = ld4(&ct.phi[c]), r = ld4(&ct.rden[c]);
+                gxr[0] = a.x; gxr[1] = a.y; gxr[2] = a.z; gxr[3] = a.w;
+                gyr[0] = bb.x; gyr[1] = bb.y; gyr[2] = bb.z; gyr[3] = bb.w;
+                phi[0] = p.x; phi[1] = p.y; phi[2] = p.z; phi[3] = p.w;
+                rden[0] = r.x; rden[1] = r.y; rden[2] = r.z; rden[3] = r.w;
+            }
         }
 #pragma unroll
         for (int v = 0; v < 4; v++) {
-            const double gx = fma(b0[2], dU[2][v], fma(b0[1], dU[1][v], b0[0] * dU[0][v]));
-            const double gy = fma(b1[2], dU[2][v], fma(b1[1], dU[1][v], b1[0] * dU[0][v]));
             double bgx = lgx[v], bgy = lgy[v];
-            if (BARTH) {
-                double np = 0.0, nn = 0.0;
-                int kp = -1, kn = -1;  // neighbour slot giving hi - Uc / lo - Uc (-1: the cell itself, 0)
-                for (int k = 0; k < 3; k++) {
-                    if (k < nnb) {
-                        if (dlt(np, dU[k][v])) { np = dU[k][v]; kp = k; }
-                        if (dlt(dU[k][v], nn)) { nn = dU[k][v]; kn = k; }
-                    }
-                }
-                double d[3];
-                for (int j = 0; j < 3; j++) d[j] = fma(gx, vx[j], gy * vy[j]);
-                int jh = 0, jl = 0;
-                double dh = d[0], dl = d[0];
+            const int cv = code >> (5 * v);
+            if (BARTH && (cv & 1)) {
+                // gx_lim = phi gx, gy_lim = phi gy, phi = num / den, den = d(vertex jj) +- eps,
+                // num = U(slot kk) - Uc
+                const int kk = ((cv >> 1) & 3) - 1, jj = (cv >> 3) & 3;
+                const double b_phi = bgx * gxr[v] + bgy * gyr[v];
+                bgx *= phi[v];
+                bgy *= phi[v];
+                const double b_num = b_phi * rden[v];
+                const double b_den = -b_phi * phi[v] * rden[v];
+                const double vxj = jj == 0 ? vx[0] : (jj == 1 ? vx[1] : vx[2]);
+                const double vyj = jj == 0 ? vy[0] : (jj == 1 ? vy[1] : vy[2]);
+                bgx = fma(b_den, vxj, bgx);
+                bgy = fma(b_den, vyj, bgy);
 #pragma unroll
-                for (int j = 1; j < 3; j++) {
-                    if (dlt(dh, d[j])) { dh = d[j]; jh = j; }
-                    if (dlt(d[j], dl)) { dl = d[j]; jl = j; }
-                }
-                const double dp = dh + kEps, dn = dl - kEps;
-                const bool lim_p = pos(dh) && dlt(np, dp);
-                const bool lim_n = neg(dl) && dlt(dn, nn);
-                if (lim_p || lim_n) {
-                    const bool use_p = lim_p && (!lim_n || dlt(nn * dp, np * dn));
-                    const double num = use_p ? np : nn, den = use_p ? dp : dn;
-                    const int kk = use_p ? kp : kn, jj = use_p ? jh : jl;
-                    const double rden = rcp(den);
-                    const double phi = num * rden;
-                    // gx_lim = phi gx, gy_lim = phi gy
-                    const double b_phi = bgx * gx + bgy * gy;
-                    bgx *= phi;
-                    bgy *= phi;
-                    const double b_num = b_phi * rden;
-                    const double b_den = -b_phi * phi * rden;
-                    // selects rather than vx[jj] / bd[kk][v]: keeps the arrays in registers
-                    const double vxj = jj == 0 ? vx[0] : (jj == 1 ? vx[1] : vx[2]);
-                    const double vyj = jj == 0 ? vy[0] : (jj == 1 ? vy[1] : vy[2]);
-                    bgx = fma(b_den, vxj, bgx);
-                    bgy = fma(b_den, vyj, bgy);
-#pragma unroll
-                    for (int k = 0; k < 3; k++)
-                        if (k == kk) bd[k][v] += b_num;
-                }
+                for (int k = 0; k < 3; k++)
+                    if (k == kk) bd[k][v] += b_num;
             }
+#pragma unroll
             for (int k = 0; k < 3; k++)
                 if (k < nnb) bd[k][v] = fma(b0[k], bgx, fma(b1[k], bgy, bd[k][v]));
         }
@@ -370,6 +354,7 @@ struct Adjoint {
     std::vector<d4*> seg_R;           // per stage of a segment's steps: the residual R(U_in)
     std::vector<double*> seg_tape;    // per stage of a segment's steps: the edge tape (kTapeFields x E)
     std::vector<int*> seg_tflags;
+    std::vector<dev::CellTape> seg_ctape;  // per stage: the limiter record (LSQ + Barth only)
     double* d_seg_dt = nullptr;    // per step: dt, dt_raw
     int* d_seg_cstar = nullptr;    // per step: the minimising cell
     d4 *d_lam = nullptr, *d_lam_in = nullptr, *d_acc0 = nullptr, *d_aL = nullptr, *d_aR = nullptr;
@@ -445,6 +430,11 @@ struct Adjoint {
         seg_tflags.assign((size_t)S * nst, nullptr);
         for (size_t i = 0; i < seg_tape.size(); i++)
             if ((rc = alloc(seg_tape[i], (size_t)dev::kTapeFields * E)) || (rc = alloc(seg_tflags[i], E))) return rc;
+        seg_ctape.assign(p.reconstruct == 3002 && p.limiter == 1 ? (size_t)S * nst : 0, dev::CellTape());
+        for (auto& t : seg_ctape)
+            if ((rc = alloc(t.gx, N)) || (rc = alloc(t.gy, N)) || (rc = alloc(t.phi, N)) || (rc = alloc(t.rden, N)) ||
+                (rc = alloc(t.code, N)))
+                return rc;
         const int nb = nblk(N, 256);
         if ((rc = alloc(d_seg_dt, 2 * (size_t)S)) || (rc = alloc(d_seg_cstar, S)) || (rc = alloc(d_lam, N)) ||
             (rc = alloc(d_lam_in, N)) || (rc = alloc(d_acc0, N)) || (rc = alloc(d_aL, E)) || (rc = alloc(d_aR, E)) ||
@@ -476,6 +466,7 @@ struct Adjoint {
             v.rec_tape.v = seg_tape[(size_t)slot * nst + si];
             v.rec_tape.flags = seg_tflags[(size_t)slot * nst + si];
             v.rec_tape.E = v.E;
+            if (!seg_ctape.empty()) v.rec_ctape = seg_ctape[(size_t)slot * nst + si];
             v.enqueue_stage(kind);
         };
         if (v.p.time_advance == 3101) {
@@ -489,6 +480,7 @@ struct Adjoint {
         }
         v.d_rec_R = nullptr;
         v.rec_tape = dev::EdgeTape();
+        v.rec_ctape = dev::CellTape();
         dev::launch_restrict(st, v.d_U, v.mv, v.d_cell_ref, v.d_cell_new, v.d_flags, v.d_flag_count, Solver::kFlagCap,
                              v.p.restrict_ref, v.gas, v.d_status);
         AK(cudaGetLastError());
@@ -497,8 +489,8 @@ struct Adjoint {
 
     // one stage VJP: lam_s (d_lam) -> lam_in (d_lam_in), acc0, partial F.mu in dot slot;
     // (Uin, Gx, Gy): the stage's input state and the limited gradients the forward used
-    int stage_vjp(const d4* Uin, const dev::EdgeTape& tape, const d4* Rs, const double* dt_p, double a, double b,
-                  int acc_mode, int dot_slot) {
+    int stage_vjp(const d4* Uin, const dev::EdgeTape& tape, const dev::CellTape& ct, const d4* Rs,
+                  const double* dt_p, double a, double b, int acc_mode, int dot_slot) {
         Solver& v = *s;
         cudaStream_t st = v.stream;
         const bool linear = v.p.reconstruct == 3002;
@@ -506,10 +498,10 @@ struct Adjoint {
         double* dp = d_dotp + (size_t)dot_slot * nbN;
         dev::k_adj_edge<<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, d_lam, d_rlist, d_aL, d_aR);
         const int* fl = tape.flags;
-        if (!linear) dev::k_adj_cell<false, false><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, fl, d_lamdir, d_bdU);
+        if (!linear) dev::k_adj_cell<false, false><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU);
         else if (v.p.limiter == 1)
-            dev::k_adj_cell<true, true><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, fl, d_lamdir, d_bdU);
-        else dev::k_adj_cell<true, false><<<nbN, 256, 0, st>>>(Uin, v.mv, d_aL, d_aR, fl, d_lamdir, d_bdU);
+            dev::k_adj_cell<true, true><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU);
+        else dev::k_adj_cell<true, false><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU);
         dev::k_adj_combine<<<nbN, 256, 0, st>>>(v.mv, d_rev, d_lamdir, d_bdU, d_lam, Rs, dt_p, a, b, acc_mode,
                                                 d_lam_in, d_acc0, linear ? 1 : 0, dp);
         AK(cudaGetLastError());
@@ -523,6 +515,9 @@ struct Adjoint {
         const double* dtp = d_seg_dt + 2 * slot;
         const int nbN = nblk(v.N, 256);
         auto R = [&](int si) { return seg_R[(size_t)slot * nst + si]; };
+        auto ctp = [&](int si) {
+            return seg_ctape.empty() ? dev::CellTape() : seg_ctape[(size_t)slot * nst + si];
+        };
         auto tp = [&](int si) {
             dev::EdgeTape t;
             t.v = seg_tape[(size_t)slot * nst + si];
@@ -534,20 +529,20 @@ struct Adjoint {
         double b0 = 1.0, b1 = 0.0, b2 = 0.0;  // b_s of the stages in reverse order
         if (v.p.time_advance == 3101) {
             // U1 = U0 + dt R(U0): a = 0, b = 1
-            if ((rc = stage_vjp(seg_states[(size_t)slot], tp(0), R(0), dtp, 0.0, 1.0, 2, 0))) return rc;
+            if ((rc = stage_vjp(seg_states[(size_t)slot], tp(0), ctp(0), R(0), dtp, 0.0, 1.0, 2, 0))) return rc;
             std::swap(d_lam, d_lam_in);
         } else {
             const d4* U0 = seg_states[(size_t)slot * 3];
             const d4* U1 = seg_states[(size_t)slot * 3 + 1];
             const d4* U2 = seg_states[(size_t)slot * 3 + 2];
             // U3 = 1/3 U0 + 2/3 (U2 + dt R(U2))
-            if ((rc = stage_vjp(U2, tp(2), R(2), dtp, 1.0 / 3.0, 2.0 / 3.0, 0, 0))) return rc;
+            if ((rc = stage_vjp(U2, tp(2), ctp(2), R(2), dtp, 1.0 / 3.0, 2.0 / 3.0, 0, 0))) return rc;
             std::swap(d_lam, d_lam_in);
             // U2 = 3/4 U0 + 1/4 (U1 + dt R(U1))
-            if ((rc = stage_vjp(U1, tp(1), R(1), dtp, 0.75, 0.25, 1, 1))) return rc;
+            if ((rc = stage_vjp(U1, tp(1), ctp(1), R(1), dtp, 0.75, 0.25, 1, 1))) return rc;
             std::swap(d_lam, d_lam_in);
             // U1 = U0 + dt R(U0); U0 also feeds stages 2 and 3 directly (acc0)
-            if ((rc = stage_vjp(U0, tp(0), R(0), dtp, 0.0, 1.0, 3, 2))) return rc;
+            if ((rc = stage_vjp(U0, tp(0), ctp(0), R(0), dtp, 0.0, 1.0, 3, 2))) return rc;
             std::swap(d_lam, d_lam_in);
             b0 = 2.0 / 3.0;
             b1 = 0.25;

@@ -218,7 +218,7 @@ void Solver::enqueue_stage(int kind) {
     cudaStream_t s = stream;
     if (needs_gradient()) {
         mark(PROF_GRAD, true);
-        dev::launch_grad(s, p.gradient, p.limiter == 1, d_U, mv, d_Gx, d_Gy);
+        dev::launch_grad(s, p.gradient, p.limiter == 1, d_U, mv, d_Gx, d_Gy, rec_ctape.gx ? &rec_ctape : nullptr);
         mark(PROF_GRAD, false);
         launches += 1;
     }

@@ -43,6 +43,7 @@ struct Solver {
     d4 *d_F = nullptr, *d_prim = nullptr, *d_rhs = nullptr, *d_res_part = nullptr;
     d4* d_rec_R = nullptr;  // when set, the update kernels also write each stage's residual here
     dev::EdgeTape rec_tape;  // when set (.v), the flux kernels also write the adjoint's edge tape
+    dev::CellTape rec_ctape;  // when set (.gx), the gradient kernel also writes the limiter record
     double *d_alpha = nullptr, *d_alpha_vis = nullptr, *d_stage = nullptr, *d_res_out = nullptr;
     int* d_flags = nullptr;
     unsigned int* d_flag_count = nullptr;

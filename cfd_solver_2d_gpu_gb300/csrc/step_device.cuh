@@ -78,9 +78,21 @@ __device__ __forceinline__ double dt_cell(int c, const MeshView& m, const double
 
 // ---- gradients and the Barth limiter (Gradient, FVMR/src/space/gradient/Gradient.cpp:116-158)
 
-template <int GRAD, bool BARTH>
+// the discrete adjoint's record of one stage's limited least-squares gradients: per cell
+// the gradient before the limiter, per variable phi and 1/den of the limiting ratio,
+// and a code word (per variable five bits: limited, the neighbour slot + 1 giving the
+// bound (0: the cell itself), the vertex)
+struct CellTape {
+    d4* gx = nullptr;
+    d4* gy = nullptr;
+    d4* phi = nullptr;
+    d4* rden = nullptr;
+    int* code = nullptr;
+};
+
+template <int GRAD, bool BARTH, bool REC = false>
 __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const MeshView& m, d4* __restrict__ Gx,
-                                          d4* __restrict__ Gy) {
+                                          d4* __restrict__ Gy, CellTape tape = CellTape()) {
     const d4 uc = ld4(&U[c]);
     const int nnb = __ldg(&m.c_nnb[c]);
     d4 un[3];
@@ -142,6 +154,16 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
             gy[v] = ginv * sy[v];
         }
     }
+    static_assert(!REC || (GRAD == 1 && BARTH), "the adjoint's record covers least squares with the Barth limiter");
+    double gxr[4], gyr[4], phiv[4] = {1, 1, 1, 1}, rdv[4] = {0, 0, 0, 0};
+    int code = 0;
+    if constexpr (REC) {
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            gxr[v] = gx[v];
+            gyr[v] = gy[v];
+        }
+    }
     if (BARTH) {
         // LimiterBarth, Gradient.cpp:58-114:
         //   phi = min over the vertices of min(1, (hi - Uc)/(d + eps)) for d > 0 and
@@ -162,17 +184,30 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
 #pragma unroll
         for (int v = 0; v < 4; v++) {
             double np = 0.0, nn = 0.0;  // hi - Uc >= 0, lo - Uc <= 0
+            int kp = -1, kn = -1;       // (REC) the slot giving np / nn, -1: the cell itself
 #pragma unroll
             for (int k = 0; k < 3; k++) {
                 if (k < nnb) {
-                    np = dmax(np, dU[k][v]);
-                    nn = dmin(nn, dU[k][v]);
+                    if constexpr (REC) {
+                        if (dlt(np, dU[k][v])) { np = dU[k][v]; kp = k; }
+                        if (dlt(dU[k][v], nn)) { nn = dU[k][v]; kn = k; }
+                    } else {
+                        np = dmax(np, dU[k][v]);
+                        nn = dmin(nn, dU[k][v]);
+                    }
                 }
             }
             const double d0 = fma(gx[v], vx[0], gy[v] * vy[0]);
             const double d1 = fma(gx[v], vx[1], gy[v] * vy[1]);
             const double d2 = fma(gx[v], vx[2], gy[v] * vy[2]);
             const double dhi = dmax(dmax(d0, d1), d2), dlo = dmin(dmin(d0, d1), d2);
+            int jh = 0, jl = 0;  // (REC) the vertices giving dhi / dlo, as dmax / dmin choose them
+            if constexpr (REC) {
+                jh = dlt(d0, d1) ? 1 : 0;
+                jh = dlt(jh ? d1 : d0, d2) ? 2 : jh;
+                jl = dlt(d1, d0) ? 1 : 0;
+                jl = dlt(d2, jl ? d1 : d0) ? 2 : jl;
+            }
             const double dp = dhi + kEps, dn = dlo - kEps;
             const bool lim_p = pos(dhi) && dlt(np, dp);  // ratio np/dp below 1
             const bool lim_n = neg(dlo) && dlt(dn, nn);  // ratio nn/dn below 1
@@ -180,7 +215,13 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
                 // both limited: np/dp < nn/dn  <=>  np*dn > nn*dp  (dp > 0 > dn)
                 const bool use_p = lim_p && (!lim_n || dlt(nn * dp, np * dn));
                 const double num = use_p ? np : nn, den = use_p ? dp : dn;
-                const double phi = num * rcp(den);
+                const double rd = rcp(den);
+                const double phi = num * rd;
+                if constexpr (REC) {
+                    phiv[v] = phi;
+                    rdv[v] = rd;
+                    code |= (1 | (((use_p ? kp : kn) + 1) << 1) | ((use_p ? jh : jl) << 3)) << (5 * v);
+                }
                 gx[v] *= phi;
                 gy[v] *= phi;
             }
@@ -188,6 +229,13 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
     }
     Gx[c] = mk4(gx[0], gx[1], gx[2], gx[3]);
     Gy[c] = mk4(gy[0], gy[1], gy[2], gy[3]);
+    if constexpr (REC) {
+        tape.gx[c] = mk4(gxr[0], gxr[1], gxr[2], gxr[3]);
+        tape.gy[c] = mk4(gyr[0], gyr[1], gyr[2], gyr[3]);
+        tape.phi[c] = mk4(phiv[0], phiv[1], phiv[2], phiv[3]);
+        tape.rden[c] = mk4(rdv[0], rdv[1], rdv[2], rdv[3]);
+        tape.code[c] = code;
+    }
 }
 
 // ---- edge fluxes: edge_convection_flux_kernel, FVMR/src/space/Flux.cpp:230-303, and

@@ -59,11 +59,11 @@ __global__ void k_dt_final(StepState* s, int advance) {
     s->dtmin_bits = (unsigned long long)__double_as_longlong(1e10);
 }
 
-template <int GRAD, bool BARTH>
+template <int GRAD, bool BARTH, bool REC>
 __global__ void __launch_bounds__(256) k_grad(const d4* __restrict__ U, MeshView m, d4* __restrict__ Gx,
-                                              d4* __restrict__ Gy) {
+                                              d4* __restrict__ Gy, CellTape tape) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < m.N) grad_cell<GRAD, BARTH>(c, U, m, Gx, Gy);
+    if (c < m.N) grad_cell<GRAD, BARTH, REC>(c, U, m, Gx, Gy, tape);
 }
 
 template <int FLUX, bool LINEAR, bool NS, bool REC>
@@ -189,15 +189,19 @@ void launch_dt(cudaStream_t s, const d4* prim, const MeshView& m, const Gas& g, 
 
 void launch_dt_final(cudaStream_t s, StepState* st, bool advance) { k_dt_final<<<1, 32, 0, s>>>(st, advance ? 1 : 0); }
 
-void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const MeshView& m, d4* Gx, d4* Gy) {
+void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const MeshView& m, d4* Gx, d4* Gy,
+                 const CellTape* tape) {
     if (m.N <= 0) return;
     const int b = blocks(m.N, 256);
-    if (gradient == 1) {
-        if (barth) k_grad<1, true><<<b, 256, 0, s>>>(U, m, Gx, Gy);
-        else k_grad<1, false><<<b, 256, 0, s>>>(U, m, Gx, Gy);
+    const CellTape none;
+    if (tape && tape->gx && gradient == 1 && barth) {  // the adjoint's recorded forward
+        k_grad<1, true, true><<<b, 256, 0, s>>>(U, m, Gx, Gy, *tape);
+    } else if (gradient == 1) {
+        if (barth) k_grad<1, true, false><<<b, 256, 0, s>>>(U, m, Gx, Gy, none);
+        else k_grad<1, false, false><<<b, 256, 0, s>>>(U, m, Gx, Gy, none);
     } else {
-        if (barth) k_grad<2, true><<<b, 256, 0, s>>>(U, m, Gx, Gy);
-        else k_grad<2, false><<<b, 256, 0, s>>>(U, m, Gx, Gy);
+        if (barth) k_grad<2, true, false><<<b, 256, 0, s>>>(U, m, Gx, Gy, none);
+        else k_grad<2, false, false><<<b, 256, 0, s>>>(U, m, Gx, Gy, none);
     }
 }
 

@@ -18,7 +18,8 @@ void launch_prim(cudaStream_t s, const d4* U, d4* U0, d4* prim, int N, const Gas
 void launch_dt(cudaStream_t s, const d4* prim, const MeshView& m, const Gas& g, double value_1, double CFL,
                bool ns, double* alpha, double* alpha_vis, unsigned long long* dtmin, Status* st);
 void launch_dt_final(cudaStream_t s, StepState* st, bool advance);
-void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const MeshView& m, d4* Gx, d4* Gy);
+void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const MeshView& m, d4* Gx, d4* Gy,
+                 const CellTape* tape = nullptr);
 void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, const d4* Gx,
                  const d4* Gy, const MeshView& m, const Gas& g, const BcData& bc, d4* F, Status* st,
                  const EdgeTape* tape = nullptr);
