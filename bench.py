@@ -504,6 +504,14 @@ def main():
             fp64 = {"achieved_gflops": a64, "peak_gflops": fp64_peak, "frac": a64 / fp64_peak,
                     "kernel": dom, "peak_source": "fvgb_fp64_peak (FMA chains, measured in this run)",
                     "source": "fp64 flop per launch from ncu x live launch time"}
+            if ncu[dom].get("fp64_inst_per_launch") and clocks.get("sm_mhz"):
+                # the FP64 pipe issues 2 thread-instructions per SM per cycle (dadd, dmul and dfma alike)
+                sms = torch.cuda.get_device_properties(local).multi_processor_count
+                peak_inst = 2 * sms * clocks["sm_mhz"] * 1e6
+                ach_inst = ncu[dom]["fp64_inst_per_launch"] / (avg_ms / 1e3)
+                fp64["issue_frac"] = ach_inst / peak_inst
+                fp64["issue_note"] = ("FP64 instructions per second over 2 x SMs x the sampled SM clock: the "
+                                      "pipe-issue bound, which counts dadd and dmul as full slots")
         stage_roof = {"achieved": stage_bytes(N, E, V) / (stage_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
                       "frac": stage_bytes(N, E, V) / (stage_ms / 1e3) / 1e9 / peak,
                       "bytes_per_stage": stage_bytes(N, E, V), "formula": "332N + 48E + 16V"}
