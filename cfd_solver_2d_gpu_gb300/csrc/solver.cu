@@ -348,18 +348,43 @@ int Solver::get_time(double* t, double* dt) {
     return 0;
 }
 
+// The device address of a page-locked host buffer (NULL for pageable memory): with
+// unified addressing the scatter / gather kernels read and write such a buffer
+// directly over the host link (NVLink-C2C on Grace), one coalesced pass and no
+// staging copy.
+static double* device_view(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? static_cast<double*>(a.devicePointer) : nullptr;
+}
+
+// returns once U has been read (GPUSolver2::host_to_device's blocking copy), so the
+// caller may reuse U at once
 int Solver::set_state(const double* U) {
-    CK(cudaMemcpyAsync(d_stage, U, (size_t)4 * N * sizeof(double), cudaMemcpyHostToDevice, stream));
-    dev::launch_scatter_in(stream, d_stage, d_U, d_cell_new, N);
+    if (const double* dv = device_view(U)) {
+        dev::launch_scatter_in(stream, dv, d_U, d_cell_new, N);
+    } else {
+        CK(cudaMemcpyAsync(d_stage, U, (size_t)4 * N * sizeof(double), cudaMemcpyHostToDevice, stream));
+        dev::launch_scatter_in(stream, d_stage, d_U, d_cell_new, N);
+    }
     launches += 1;
     CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(stream));
     return 0;
 }
 
 int Solver::get_state(double* U) {
-    dev::launch_gather_out(stream, d_U, d_stage, d_cell_new, N);
+    if (double* dv = device_view(U)) {
+        dev::launch_gather_out(stream, d_U, dv, d_cell_new, N);
+    } else {
+        dev::launch_gather_out(stream, d_U, d_stage, d_cell_new, N);
+        CK(cudaMemcpyAsync(U, d_stage, (size_t)4 * N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    }
     launches += 1;
-    CK(cudaMemcpyAsync(U, d_stage, (size_t)4 * N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(stream));
     return 0;
 }

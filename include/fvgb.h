@@ -155,7 +155,9 @@ int fvgb_find_continue_file(const char* directory, const char* name, char* path_
 int fvgb_create(const fvgb_mesh_soa* mesh, const fvgb_params* p, fvgb_handle** out);
 void fvgb_destroy(fvgb_handle* h);
 /* host <-> device state, reference numbering (GPUSolver2::host_to_device /
- * device_to_host, GPUSolver2.cpp:222-239). */
+ * device_to_host, GPUSolver2.cpp:222-239).  Both return once U has been read or
+ * written.  A page-locked U (cudaHostAlloc / cudaHostRegister) is read and written
+ * by the permuting kernels directly over the host link, with no staging copy. */
 int fvgb_set_state(fvgb_handle* h, const double* U);
 int fvgb_get_state(fvgb_handle* h, double* U);
 /* nsteps of CIteration::iteration_device (FVMR/src/time/CIteration.cpp:89-161):
