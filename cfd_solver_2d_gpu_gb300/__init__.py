@@ -124,6 +124,7 @@ def lib():
             "fvgb_batch_tune": (i, [v, i, c, i]),
             "fvgb_batch_info": (i, [v, ctypes.POINTER(ctypes.c_longlong)]),
             "fvgb_fp64_peak": (i, [i, dp]),
+            "fvgb_barrier_selftest": (i, [i, i, i, ctypes.c_longlong, ip, ip]),
             "fvgb_node_field": (i, [v, dp]),
             "fvgb_boundary_forces": (i, [v, dp, dp, dp, dp]),
             "fvgb_write_tecplot_volume": (i, [v, c, c, d, i]),
@@ -245,6 +246,14 @@ def find_continue_file(directory, name):
         return None
     _check(rc)
     return os.fsdecode(buf.value)
+
+
+def barrier_selftest(blocks=8, absent_block=-1, spin_limit=200000, device=0):
+    """fvgb_barrier_selftest: (timed_out, blocks whose wait succeeded)."""
+    t, passed = ctypes.c_int(), ctypes.c_int()
+    _check(lib().fvgb_barrier_selftest(int(device), int(blocks), int(absent_block), int(spin_limit),
+                                       ctypes.byref(t), ctypes.byref(passed)))
+    return bool(t.value), passed.value
 
 
 def fp64_peak(device=0):

@@ -569,3 +569,49 @@ extern "C" int fvgb_batch_info(fvgb_batch* h, long long out[8]) {
     out[7] = h->b.use_graph ? 1 : 0;
     return 0;
 }
+
+// ---- the bounded barrier's give-up path, exercised without a fault ---------------
+namespace fvgb {
+namespace dev {
+// every block but `absent` meets at grid_sync with the given poll limit; `absent`
+// returns at once, so with absent >= 0 the others must give up and set the error word
+__global__ void k_barrier_probe(GridBarrier* b, long long limit, int absent, int* passed) {
+    if ((int)blockIdx.x == absent) return;
+    const bool ok = grid_sync(b, limit);
+    if (threadIdx.x == 0 && ok) atomicAdd(passed, 1);
+}
+}  // namespace dev
+}  // namespace fvgb
+
+extern "C" int fvgb_barrier_selftest(int device, int blocks, int absent_block, long long spin_limit, int* timed_out,
+                                     int* blocks_passed) {
+    using namespace fvgb;
+    if (!timed_out || blocks <= 0 || blocks > 64 || spin_limit <= 0 || absent_block >= blocks)
+        return fail(FVGB_ERR_ARG, "bad arguments");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(FVGB_ERR_NO_DEVICE, "no CUDA device");
+    BK(cudaSetDevice(device));
+    dev::GridBarrier* bar = nullptr;
+    int* passed = nullptr;
+    BK(cudaMalloc(&bar, sizeof(dev::GridBarrier)));
+    if (cudaMalloc(&passed, sizeof(int)) != cudaSuccess) {
+        cudaFree(bar);
+        return fail(FVGB_ERR_CUDA, "cudaMalloc failed");
+    }
+    cudaMemset(bar, 0, sizeof(dev::GridBarrier));
+    cudaMemset(passed, 0, sizeof(int));
+    // a handful of 32-thread blocks: all resident at once
+    dev::k_barrier_probe<<<blocks, 32>>>(bar, spin_limit, absent_block, passed);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    dev::GridBarrier hb{};
+    int hp = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&hb, bar, sizeof hb, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&hp, passed, sizeof hp, cudaMemcpyDeviceToHost);
+    cudaFree(bar);
+    cudaFree(passed);
+    if (e != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("barrier probe: ") + cudaGetErrorString(e));
+    *timed_out = hb.error ? 1 : 0;
+    if (blocks_passed) *blocks_passed = hp;
+    return 0;
+}

@@ -45,8 +45,10 @@ struct BatchView {
 
 constexpr long long kBarrierSpinLimit = 20000000;  // ~0.6 s of 32 ns sleeps, far above any phase here
 
-// bounded sense-reversal barrier over all blocks of a cooperative launch
-__device__ __forceinline__ bool grid_sync(GridBarrier* b) {
+// bounded sense-reversal barrier over all blocks of a cooperative launch: a block that
+// waits more than `limit` polls (or sees another's give-up) sets the error word and
+// returns false, so a missing block ends the kernel instead of hanging it
+__device__ __forceinline__ bool grid_sync(GridBarrier* b, long long limit = kBarrierSpinLimit) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -62,7 +64,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b) {
         } else {
             long long it = 0;
             while (*vgen == g) {
-                if (++it > kBarrierSpinLimit || *(volatile unsigned int*)&b->error) {
+                if (++it > limit || *(volatile unsigned int*)&b->error) {
                     atomicExch(&b->error, 1u);
                     ok = 0;
                     break;

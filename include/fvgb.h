@@ -274,6 +274,13 @@ int fvgb_batch_step_timed(fvgb_batch* b, int nsteps, double* ms_out);
  * schedule on trial_steps steps of this batch (state restored afterwards) and
  * keeps the fastest; report gets one line per candidate. */
 int fvgb_batch_tune(fvgb_batch* b, int trial_steps, char* report, int report_len);
+/* The persistent kernel's bounded grid barrier, exercised on its own: `blocks`
+ * 32-thread blocks meet at one barrier with at most spin_limit polls each; block
+ * absent_block (-1: none) never arrives, so the others give up, set the error word
+ * and return.  *timed_out = that error word, *blocks_passed = the blocks whose wait
+ * succeeded.  The GPU stays usable either way (nothing faults, every wait ends). */
+int fvgb_barrier_selftest(int device, int blocks, int absent_block, long long spin_limit, int* timed_out,
+                          int* blocks_passed);
 /* [0] instances, [1] cells, [2] edges, [3] grid, [4] block, [5] kernel
  * launches, [6] tile size (negative: queued schedule), [7] 1 if the step runs
  * as a captured graph. */

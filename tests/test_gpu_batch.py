@@ -79,3 +79,15 @@ def test_batch_rejects_mixed_schemes(tmp_path):
     c = cylinders(tmp_path, [5], [0.2], flux=2001)[0]
     with pytest.raises(fv.FvgbError):
         fv.Batch([a[0], c[0]], [a[1], c[1]])
+
+
+def test_bounded_barrier_gives_up_and_reports():
+    """A block that never arrives makes the others' bounded wait run out: they set the error
+    word and return (no hang, no fault), and the GPU stays usable."""
+    import time
+    t0 = time.perf_counter()
+    timed_out, passed = fv.barrier_selftest(blocks=8, absent_block=3, spin_limit=200000)
+    assert timed_out and passed == 0
+    assert time.perf_counter() - t0 < 5.0
+    timed_out, passed = fv.barrier_selftest(blocks=8, absent_block=-1, spin_limit=200000)
+    assert not timed_out and passed == 8
