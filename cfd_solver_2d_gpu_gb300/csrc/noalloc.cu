@@ -30,9 +30,11 @@ namespace {
 constexpr int kNoallocMaxEdges = 1 << 20;   // 1,048,576 edges -> 4 doubles each = 32 MiB
 constexpr int kMaxDevices = 64;
 
-__device__ __align__(256) double g_noalloc_edge_flux[4 * (size_t)kNoallocMaxEdges];
+static __device__ __align__(256) double g_noalloc_edge_flux[4 * (size_t)kNoallocMaxEdges];
 
 // host-side addresses of the array, looked up once per device with that device current
+// (in host code the array's name is only a stand-in, never a device address); the
+// first call on a device does this look-up, so it belongs before any stream capture
 std::mutex g_addr_mu;
 double* g_addr[kMaxDevices] = {};
 
