@@ -8,6 +8,7 @@ FVMR/src/input/TomlFileManager.cpp:110-170, plus the [gpu] table).
     vortex_adjoint 256 x 256 jittered vortex, 131,072 cells, LSQ + Barth, Roe, SSP-RK3
 """
 import os
+import re
 import tempfile
 
 from . import write_cylinder, write_periodic_square
@@ -28,7 +29,9 @@ def _num(x):
 def toml_text(*, equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=3103, CFL=0.5,
               T_end=1000.0, ic_type=2, vortex=(5.0, 5.0, 5.0), inf_mode=1, inf=(1.0, 1.0, 1.0, 1.0), Ma=0.2,
               AoA=0.0, Re=None, mu0=17.9e-6, Pr=0.72, ref_area=1.0, lsq_det="ref", wall_bc="ref", restrict="ref",
-              renumber=1, filename="mesh", max_iteration=1000):
+              renumber=1, filename="mesh", max_iteration=1000, inlet=None, outlet=None):
+    """inlet / outlet: None (table left out, the reference's default state), (rho, u, v, p)
+    (input_mode 1) or (Ma, AoA) (input_mode 0), as [boundaryCondition.2D.inlet|outlet]."""
     lines = [
         "[basic]", "continue = false", "dimension = 2", f'filename = "{filename}"', 'meshFileType = "su2"',
         "useGPU = 1", "isDebugMode = false", "",
@@ -47,6 +50,14 @@ def toml_text(*, equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1,
         lines += ["input_mode = 1", f"rho = {_num(inf[0])}", f"u = {_num(inf[1])}", f"v = {_num(inf[2])}", f"p = {_num(inf[3])}"]
     else:
         lines += ["input_mode = 0", f"Ma = {_num(Ma)}", f"AoA = {_num(AoA)}"]
+    for name, bc in (("inlet", inlet), ("outlet", outlet)):
+        if bc is None:
+            continue
+        lines += ["", f"[boundaryCondition.2D.{name}]"]
+        if len(bc) == 4:
+            lines += ["input_mode = 1"] + [f"{k} = {_num(v)}" for k, v in zip(("rho", "u", "v", "p"), bc)]
+        else:
+            lines += ["input_mode = 0", f"Ma = {_num(bc[0])}", f"AoA = {_num(bc[1])}"]
     lines += ["", "[output]", "step_per_print = 50", "step_per_output_field = 100", "step_per_output_hist = 100",
               f"maxIteration = {max_iteration}", "tolerace_residual = 1e-7", "",
               "[physicsModel]", f"equation = {equation}", "",
@@ -70,6 +81,22 @@ def square_mesh(n, jitter=0.0, L=10.0, seed=JITTER_SEED, directory=None):
     if not os.path.exists(path):
         tmp = path + f".{os.getpid()}.tmp"
         write_periodic_square(tmp, n, L, jitter, seed)
+        os.replace(tmp, path)
+    return path
+
+
+def channel_mesh(n, jitter=0.0, L=10.0, seed=JITTER_SEED, directory=None):
+    """The square of square_mesh with its four boundaries renamed: inlet (x = 0),
+    outlet (x = L), symmetry (y = L) and wall (y = 0; slip for Euler, no-slip
+    adiabatic for Navier-Stokes)."""
+    path = os.path.join(cache_dir(directory), f"channel_{n}_{jitter:g}_{seed}.su2")
+    if not os.path.exists(path):
+        text = open(square_mesh(n, jitter, L, seed, directory)).read()
+        tags = iter(("inlet", "outlet", "symmetry", "wall"))  # the square's marker order: left, right, top, bottom
+        text = re.sub(r"MARKER_TAG= periodic_\d", lambda _: "MARKER_TAG= " + next(tags), text)
+        tmp = path + f".{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
+            f.write(text)
         os.replace(tmp, path)
     return path
 

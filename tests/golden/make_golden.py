@@ -3,7 +3,7 @@ itself: the reference's CPU step path compiled from its own sources with
 myfloat = double (oracle/ref, binary oracle/_ref/fvmr_ref_f64).
 
 Run here, where the reference sources are present:
-    make -C oracle/ref && python tests/golden/make_golden.py
+    make -C oracle/ref && python tests/golden/make_golden.py [fixture names]
 
 Each fixture is one compressed .npz with the case's input.toml text, the mesh
 (.su2 text, compressed), the reference's mesh arrays, its initial field, one
@@ -40,6 +40,7 @@ def golden_cases(d):
     sq24j = cases.square_mesh(24, jitter=0.2, directory=d)
     sq64 = cases.square_mesh(64, directory=d)
     cyl = cases.cylinder_mesh(32, 16, directory=d)
+    ch24j = cases.channel_mesh(24, jitter=0.2, directory=d)
     T = cases.toml_text
     return [
         # the small plain config: 64x64 vortex, Roe, first order, Kutta RK3, CFL 0.5, 1000 steps
@@ -65,6 +66,23 @@ def golden_cases(d):
         # inviscid cylinder: slip wall, far field
         ("cylinder32_euler_roe_lsq_rk3", T(equation=1, flux=2002, reconstruct=3002, gradient=1, limiter=1,
                                            time_advance=3103, CFL=0.5, ic_type=1, inf_mode=0, Ma=0.5), cyl, "rk3", 5),
+        # channel: inlet (x = 0), outlet (x = 10), symmetry (y = 10), wall (y = 0); the vortex sits
+        # near two of them so that their edges see a non-uniform state
+        # subsonic inflow and outflow, slip wall
+        ("jchannel24_roe_lsq_barth_ssp", T(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104,
+                                           CFL=0.8, vortex=(2.5, 7.0, 5.0), inf=(1.0, 1.0, 0.3, 1.0),
+                                           inlet=(1.0, 1.0, 0.3, 1.0), outlet=(1.0, 1.0, 0.0, 0.9)),
+         ch24j, "ssprk3", 10),
+        # supersonic inflow and outflow (Mach 2.1)
+        ("jchannel24_llf_lsq_barth_rk3_mach2", T(flux=2001, reconstruct=3002, gradient=1, limiter=1,
+                                                 time_advance=3103, CFL=0.5, vortex=(7.0, 3.0, 3.0),
+                                                 inf=(1.0, 2.5, 0.2, 1.0), inlet=(1.0, 2.5, 0.2, 1.0),
+                                                 outlet=(1.0, 2.5, 0.0, 1.0)), ch24j, "rk3", 10),
+        # laminar: no-slip adiabatic wall, Green-Gauss gradients, viscous fluxes on every boundary kind
+        ("jchannel24_ns_gg_barth_rk3", T(equation=2, flux=2002, reconstruct=3002, gradient=2, limiter=1,
+                                         time_advance=3103, CFL=0.5, vortex=(5.0, 2.5, 5.0), inf=(1.0, 1.0, 0.3, 1.0),
+                                         Re=100.0, inlet=(1.0, 1.0, 0.3, 1.0), outlet=(1.0, 1.0, 0.0, 0.9)),
+         ch24j, "rk3", 5),
     ]
 
 
@@ -152,11 +170,15 @@ def run_ref(binary, toml_path, su2, mode, steps, out):
     return read_dump(out)
 
 
-def main():
+def main(only=()):
+    """Makes every fixture, or with names on the command line only the step fixtures of
+    those names (existing files are then left as they are)."""
     if not os.path.exists(REF):
         sys.exit("build the reference first: make -C oracle/ref")
     with tempfile.TemporaryDirectory() as d:
         for name, toml, su2, mode, steps in golden_cases(d):
+            if only and name not in only:
+                continue
             tp = os.path.join(d, name + ".toml")
             with open(tp, "w") as f:
                 f.write(toml)
@@ -174,8 +196,9 @@ def main():
             path = os.path.join(HERE, name + ".npz")
             np.savez_compressed(path, **out)
             print(f"{path}: N={rhs['sizes'][0]} {mode} x{steps} ({os.path.getsize(path) // 1024} KiB)")
-        make_continue(d)
-        make_output(d)
+        if not only:
+            make_continue(d)
+            make_output(d)
 
 
 def load(name):
@@ -197,4 +220,4 @@ def names():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -60,6 +60,25 @@ def test_batch_matches_plain_vortex_ssp_gg_llf(tmp_path):
         assert np.array_equal(b.get_state(i), U), i
 
 
+def test_batch_matches_plain_channels(tmp_path):
+    """Inlet, outlet, symmetry and slip-wall edges, each instance with its own inflow and
+    outflow states (one supersonic)."""
+    inst = []
+    for i, (n, inlet, outlet) in enumerate(((8, (1.0, 1.0, 0.3, 1.0), (1.0, 1.0, 0.0, 0.9)),
+                                            (16, (1.0, 2.5, 0.2, 1.0), (1.0, 2.5, 0.0, 1.0)),
+                                            (12, (1.2, 0.6, -0.1, 1.1), (0.9, 0.5, 0.0, 1.0)))):
+        tp, sp = cases.write_case(str(tmp_path), f"ch{i}", cases.toml_text(
+            flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3103, CFL=0.5, vortex=(2.5, 7.0, 3.0),
+            inf=inlet, inlet=inlet, outlet=outlet), cases.channel_mesh(n, jitter=0.2, directory=str(tmp_path)))
+        inst.append(load(tp, sp))
+    b = fv.Batch([m for m, _ in inst], [p for _, p in inst])
+    t = b.step(3)
+    for i, (m, p) in enumerate(inst):
+        U, tp = plain_run(m, p, 3)
+        assert np.array_equal(b.get_state(i), U), i
+        assert t[i] == tp
+
+
 def test_autotuner_keeps_state_and_result(tmp_path):
     inst = cylinders(tmp_path, [8, 14, 5], [0.1, 0.4, 0.6])
     b = fv.Batch([m for m, _ in inst], [p for _, p in inst])

@@ -57,7 +57,8 @@ def test_toml_matches_reference_semantics(name):
         assert getattr(p, k) == getattr(q, k), k
     for k in ("gamma", "R", "Pr", "mu0", "T0", "CFL", "T_end"):
         assert getattr(p, k) == pytest.approx(getattr(q, k), rel=1e-15), k
-    assert np.allclose(list(p.inf), list(q.inf), rtol=1e-15, atol=0)
+    for k in ("inf", "inlet", "outlet"):
+        assert np.allclose(list(getattr(p, k)), list(getattr(q, k)), rtol=1e-15, atol=0), k
 
 
 REF_TOML = "/root/reference/quick_start/U2NITS-10.0"
@@ -121,3 +122,21 @@ def test_cases_write_valid_toml(tmp_path):
     tp, sp = cases.vortex_small(str(tmp_path), n=8)
     p = fv.Params.from_toml(tp)
     assert (p.time_advance, p.reconstruct, p.CFL) == (3103, 3001, 0.5)
+
+
+def test_channel_boundaries_and_inlet_tables(tmp_path):
+    """Boundary names to types (BoundaryManager.cpp:15-48: "wall" is slip for Euler, no-slip
+    adiabatic for Navier-Stokes) and the inlet / outlet tables in both input modes
+    (TomlFileManager.cpp:200-265), against the oracle's reading of the same file."""
+    sp = cases.channel_mesh(6, directory=str(tmp_path))
+    assert list(fv.Mesh.read_su2(sp, equation=1).array("boundary_type")) == [6011, 6012, 6021, 6001]
+    assert list(fv.Mesh.read_su2(sp, equation=2).array("boundary_type")) == [6011, 6012, 6021, 6002]
+    tp = tmp_path / "ch.toml"
+    tp.write_text(cases.toml_text(inlet=(0.4, 10.0), outlet=(1.2, 0.5, -0.1, 0.8)))
+    p = fv.Params.from_toml(str(tp))
+    q, _ = params_from_toml(str(tp))
+    assert list(p.outlet) == [1.2, 0.5, -0.1, 0.8]
+    assert np.allclose(list(p.inlet), list(q.inlet), rtol=1e-15, atol=0)
+    # (Ma, AoA) with T0, p0 the stagnation state: flow at 10 degrees, static pressure below p0
+    assert np.degrees(np.arctan2(p.inlet[2], p.inlet[1])) == pytest.approx(10.0, rel=1e-12)
+    assert p.inlet[3] < 101325.0
