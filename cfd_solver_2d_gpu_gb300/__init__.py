@@ -38,7 +38,8 @@ class Params(ctypes.Structure):
         (n, ctypes.c_double) for n in ("gamma", "R", "Pr", "mu0", "T0", "CFL", "T_end", "Re")] + [
         ("inf", ctypes.c_double * 4), ("inlet", ctypes.c_double * 4), ("outlet", ctypes.c_double * 4),
         ("vortex", ctypes.c_double * 3), ("shock", ctypes.c_double * 4), ("mesh_scale", ctypes.c_double),
-        ("max_iteration", ctypes.c_int), ("pad_", ctypes.c_int), ("ref_area", ctypes.c_double)]
+        ("max_iteration", ctypes.c_int), ("pad_", ctypes.c_int), ("ref_area", ctypes.c_double),
+        ("dsr", ctypes.c_double * 3), ("dsr_time", ctypes.c_double)]
 
     @classmethod
     def default(cls):

@@ -29,9 +29,12 @@ def _num(x):
 def toml_text(*, equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=3103, CFL=0.5,
               T_end=1000.0, ic_type=2, vortex=(5.0, 5.0, 5.0), inf_mode=1, inf=(1.0, 1.0, 1.0, 1.0), Ma=0.2,
               AoA=0.0, Re=None, mu0=17.9e-6, Pr=0.72, ref_area=1.0, lsq_det="ref", wall_bc="ref", restrict="ref",
-              renumber=1, filename="mesh", max_iteration=1000, inlet=None, outlet=None):
+              renumber=1, filename="mesh", max_iteration=1000, inlet=None, outlet=None, shock_tube=None, dmr=None):
     """inlet / outlet: None (table left out, the reference's default state), (rho, u, v, p)
-    (input_mode 1) or (Ma, AoA) (input_mode 0), as [boundaryCondition.2D.inlet|outlet]."""
+    (input_mode 1), (rho, u, angle_degree, p, "angle") (input_mode 3) or (Ma, AoA)
+    (input_mode 0), as [boundaryCondition.2D.inlet|outlet].  shock_tube: (x, y, normal x,
+    normal y) of [initialCondition.shockTube]; dmr: (x, y, angle) of
+    [initialCondition.doubleShockReflection]."""
     lines = [
         "[basic]", "continue = false", "dimension = 2", f'filename = "{filename}"', 'meshFileType = "su2"',
         "useGPU = 1", "isDebugMode = false", "",
@@ -45,6 +48,12 @@ def toml_text(*, equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1,
     if ic_type == 2:
         lines += ["[initialCondition.isentropicVortex]", f"vortex_x = {_num(vortex[0])}", f"vortex_y = {_num(vortex[1])}",
                   f"vortex_strength = {_num(vortex[2])}"]
+    if shock_tube is not None:
+        lines += ["[initialCondition.shockTube]"] + [f"{k} = {_num(v)}" for k, v in zip(
+            ("shock_x", "shock_y", "shock_normal_x", "shock_normal_y"), shock_tube)]
+    if dmr is not None:
+        lines += ["[initialCondition.doubleShockReflection]"] + [f"{k} = {_num(v)}" for k, v in zip(
+            ("shock_x", "shock_y", "shock_angle_degree"), dmr)]
     lines += ["", "[boundaryCondition.2D.inf]"]
     if inf_mode == 1:
         lines += ["input_mode = 1", f"rho = {_num(inf[0])}", f"u = {_num(inf[1])}", f"v = {_num(inf[2])}", f"p = {_num(inf[3])}"]
@@ -56,6 +65,8 @@ def toml_text(*, equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1,
         lines += ["", f"[boundaryCondition.2D.{name}]"]
         if len(bc) == 4:
             lines += ["input_mode = 1"] + [f"{k} = {_num(v)}" for k, v in zip(("rho", "u", "v", "p"), bc)]
+        elif len(bc) == 5:
+            lines += ["input_mode = 3"] + [f"{k} = {_num(v)}" for k, v in zip(("rho", "u", "angle_degree", "p"), bc)]
         else:
             lines += ["input_mode = 0", f"Ma = {_num(bc[0])}", f"AoA = {_num(bc[1])}"]
     lines += ["", "[output]", "step_per_print = 50", "step_per_output_field = 100", "step_per_output_hist = 100",
@@ -98,6 +109,53 @@ def channel_mesh(n, jitter=0.0, L=10.0, seed=JITTER_SEED, directory=None):
         with open(tmp, "w") as f:
             f.write(text)
         os.replace(tmp, path)
+    return path
+
+
+def dmr_mesh(nx, jitter=0.0, wall="wall", seed=JITTER_SEED, directory=None):
+    """The double-Mach-reflection domain [0, 4] x [0, 1] as nx x nx/4 quads (nx a
+    multiple of 24, so that a node sits at x = 1/6).  Markers: "inlet" (x = 0, and
+    y = 0 for x < 1/6), "outlet" (x = 4), "dsr" (y = 1) and `wall` (y = 0 from
+    x = 1/6).  Interior nodes are moved by up to +-jitter h in x and y (seeded)."""
+    import numpy as np
+    if nx % 24:
+        raise ValueError("nx must be a multiple of 24")
+    ny = nx // 4
+    path = os.path.join(cache_dir(directory), f"dmr_{nx}_{jitter:g}_{wall}_{seed}.su2")
+    if os.path.exists(path):
+        return path
+    h = 4.0 / nx
+    xs, ys = np.meshgrid(np.arange(nx + 1) * h, np.arange(ny + 1) * h)  # node (i, j) at index j (nx + 1) + i
+    rng = np.random.default_rng(seed)
+    d = rng.uniform(-jitter * h, jitter * h, (2, ny + 1, nx + 1))
+    d[:, [0, -1], :] = 0.0
+    d[:, :, [0, -1]] = 0.0
+    xs, ys = xs + d[0], ys + d[1]
+    nid = lambda i, j: j * (nx + 1) + i
+    lines = ["%% double Mach reflection domain [0,4]x[0,1], %d x %d quads, jitter %g h, seed %d" % (nx, ny, jitter, seed),
+             "NDIME= 2", "NELEM= %d" % (nx * ny)]
+    k = 0
+    for j in range(ny):
+        for i in range(nx):
+            lines.append("9 %d %d %d %d %d" % (nid(i, j), nid(i + 1, j), nid(i + 1, j + 1), nid(i, j + 1), k))
+            k += 1
+    lines.append("NPOIN= %d" % ((nx + 1) * (ny + 1)))
+    for j in range(ny + 1):
+        for i in range(nx + 1):
+            lines.append("%.17g %.17g %d" % (xs[j, i], ys[j, i], nid(i, j)))
+    i_w = nx // 24
+    markers = [("inlet", [(nid(0, j + 1), nid(0, j)) for j in reversed(range(ny))] +
+                [(nid(i, 0), nid(i + 1, 0)) for i in range(i_w)]),
+               ("outlet", [(nid(nx, j), nid(nx, j + 1)) for j in range(ny)]),
+               ("dsr", [(nid(i + 1, ny), nid(i, ny)) for i in reversed(range(nx))]),
+               (wall, [(nid(i, 0), nid(i + 1, 0)) for i in range(i_w, nx)])]
+    lines.append("NMARK= %d" % len(markers))
+    for name, edges in markers:
+        lines += ["MARKER_TAG= " + name, "MARKER_ELEMS= %d" % len(edges)] + ["3 %d %d" % e for e in edges]
+    tmp = path + f".{os.getpid()}.tmp"
+    with open(tmp, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    os.replace(tmp, path)
     return path
 
 

@@ -378,10 +378,6 @@ struct Batch {
             return rc;
         if (p.gradient == 2 && ((rc = upload(d_gg, gg)) || (rc = upload(d_ginv, ginv)) || (rc = upload(d_ggout, ggout))))
             return rc;
-        std::vector<dev::BcData> bcs(n);
-        for (int i = 0; i < n; i++) bcs[i] = make_bc(params[i]);
-        dev::BcData* d_bc;
-        if ((rc = upload(d_bc, bcs))) return rc;
         dev::MeshView& m = bv.m;
         m.N = N;
         m.E = E;
@@ -405,7 +401,6 @@ struct Batch {
         bv.n_inst = n;
         bv.c_inst = d_cinst;
         bv.e_inst = d_einst;
-        bv.bc = d_bc;
         bv.cell_key = d_key;
         bv.dev_of_key = d_dok;
         if ((rc = alloc(bv.U, N)) || (rc = alloc(bv.U0, N)) || (rc = alloc(bv.Gx, N)) || (rc = alloc(bv.Gy, N)) ||
@@ -419,6 +414,17 @@ struct Batch {
             bv.K1 = bv.U0;
         }
         bv.inst = d_inst;
+        {  // boundary data per instance; the double-Mach-reflection clock is the instance's
+            std::vector<dev::BcData> bcs(n);
+            for (int i = 0; i < n; i++) {
+                bcs[i] = make_bc(params[i]);
+                bcs[i].clock_t0 = &d_inst[i].t_old;
+                bcs[i].clock_dt = &d_inst[i].dt;
+            }
+            dev::BcData* d_bc;
+            if ((rc = upload(d_bc, bcs))) return rc;
+            bv.bc = d_bc;
+        }
         bv.flag_cap = kFlagCap;
         bv.bar = d_bar;
         bv.tile = 256;
@@ -447,7 +453,7 @@ struct Batch {
         if ((rc = size_grid())) return rc;
         // initial fields
         for (int i = 0; i < n; i++) {
-            if (params[i].ic_type < 1 || params[i].ic_type > 3) continue;
+            if (params[i].ic_type < 1 || params[i].ic_type > 4) continue;
             std::vector<double> U0((size_t)4 * layouts[i].N);
             if ((rc = initial_field(*meshes[i], params[i], U0.data()))) return rc;
             if ((rc = set_state(i, U0.data()))) return rc;

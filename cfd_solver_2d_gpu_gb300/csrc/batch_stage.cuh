@@ -11,7 +11,7 @@ namespace dev {
 struct InstState {
     double t, T, dt, dt6, dt_raw, CFL;
     unsigned long long dtmin_bits;
-    unsigned long long pad;
+    double t_old;  // t at the start of the step (the clock of the double-Mach-reflection boundary)
 };
 
 struct GridBarrier {
@@ -146,6 +146,7 @@ __global__ void k_batch_stage(BatchView bv, Gas g) {
             double dt = __longlong_as_double((long long)s.dtmin_bits);
             s.dt_raw = dt;
             if (s.t + dt > s.T) dt = s.T - s.t;
+            s.t_old = s.t;
             s.t += dt;
             s.dt = dt;
             s.dt6 = dt / 6.0;
@@ -161,7 +162,8 @@ __global__ void k_batch_stage(BatchView bv, Gas g) {
         if (e < m.E_int) {
             flux_interior<FLUX, LINEAR, false>(e, bv.U, bv.Gx, bv.Gy, m, g, bv.F);
         } else {
-            const BcData bc = bv.bc[__ldg(&bv.e_inst[e])];
+            BcData bc = bv.bc[__ldg(&bv.e_inst[e])];
+            bc.clock_frac = dsr_stage_frac(KIND);
             flux_boundary<FLUX, LINEAR, false>(e, bv.U, bv.Gx, bv.Gy, m, g, bc, bv.F, bv.status);
         }
     });

@@ -489,6 +489,21 @@ int initial_field(const fvgb_mesh_soa& s, const fvgb_params& p, double* U) {
         }
         return 0;
     }
+    case 4: {  // setInitialDoubleShockReflection, FieldInitializer.cpp:224-260: upstream of the
+               // shock line (CBoundaryDoubleShockReflect::isUpStreamOfShock_forElement,
+               // CBoundaryDoubleShockReflect.cpp:17-33) takes the inlet state
+        const double angle = p.dsr[2] * kPi / 180.0;
+        const double nxs = -std::sin(angle), nys = std::cos(angle);
+        double ui[4], uo[4];
+        ruvp_to_U(p.inlet, ui, gamma);
+        ruvp_to_U(p.outlet, uo, gamma);
+        for (int e = 0; e < N; e++) {
+            const double rx = s.elem_xy[e] - p.dsr[0], ry = s.elem_xy[(size_t)N + e] - p.dsr[1];
+            const bool upstream = rx * nxs + ry * nys > 0;
+            for (int j = 0; j < 4; j++) U[(size_t)j * N + e] = upstream ? ui[j] : uo[j];
+        }
+        return 0;
+    }
     default:
         return fail(FVGB_ERR_UNSUPPORTED, "initialCondition.type not supported on this path");
     }

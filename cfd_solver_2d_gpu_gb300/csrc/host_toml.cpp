@@ -245,6 +245,8 @@ extern "C" int fvgb_params_default(fvgb_params* p) {
     p->T_end = 20;
     p->Re = 1.0e8;
     p->vortex[2] = 1;
+    p->shock[2] = 1.0;  // FieldInitializer.h:23-26: the shock normal points along +x
+    p->dsr[2] = 60.0;   // CBoundaryDoubleShockReflect.h:14
     p->mesh_scale = 1.0;
     p->max_iteration = 5000;
     p->ref_area = 1.0;
@@ -299,6 +301,13 @@ extern "C" int fvgb_params_read_toml(const char* path, fvgb_params* p, char* mes
         r.num("initialCondition.shockTube.shock_y", p->shock[1], false);
         r.num("initialCondition.shockTube.shock_normal_x", p->shock[2], false);
         r.num("initialCondition.shockTube.shock_normal_y", p->shock[3], false);
+    }
+    if (p->ic_type == 4) {  // FieldInitializer::initialize_using_config, FieldInitializer.cpp:93-108
+        r.num("initialCondition.doubleShockReflection.shock_x", p->dsr[0], true);
+        r.num("initialCondition.doubleShockReflection.shock_y", p->dsr[1], true);
+        r.num("initialCondition.doubleShockReflection.shock_angle_degree", p->dsr[2], true);
+        if (p->dsr[2] > 90 || p->dsr[2] < 0)
+            return fail(FVGB_ERR_FORMAT, "shock_angle_degree out of range [0,90]");
     }
     {  // read_mu0_Re_from_config, TomlFileManager.cpp:79-104
         double rho_ref, U_ref;

@@ -38,6 +38,14 @@ struct BcData {
     double a_inf, a_inlet, a_outlet;       // sound speeds sqrt(gamma p / rho)
     double son_inf, son_inlet, son_outlet; // p / rho^gamma
     int wall_ref;                          // 1: the reference's no-slip ghost state
+    // double Mach reflection ("dsr" edges): the far-field state is the inlet's upstream of
+    // the moving shock and the outlet's downstream of it; the shock meets the boundary at
+    // x = dsr_x + (y + 20 t) / sqrt3, t being the stage's time
+    // *clock_t0 + clock_frac * *clock_dt (device words; null where no "dsr" edge exists)
+    double dsr_x, sqrt3;
+    const double* clock_t0;
+    const double* clock_dt;
+    double clock_frac;
 };
 
 // Status words written by the kernels (never a trap).

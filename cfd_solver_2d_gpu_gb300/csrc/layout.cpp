@@ -85,9 +85,6 @@ int build_layout(const fvgb_mesh_soa& m, const fvgb_params& p, Layout& L) {
     for (int i = 0; i < E; i++) L.edge_new[L.edge_ref[i]] = i;
     L.E_int = 0;
     while (L.E_int < E && bc_of(L.edge_ref[L.E_int]) == BC_INTERIOR) L.E_int++;
-    for (int s = 0; s < m.num_boundary; s++)
-        if (m.boundary_type[s] == BC_DSR)
-            return fail(FVGB_ERR_UNSUPPORTED, "double-Mach-reflection boundary is outside this path");
 
     // ---- per-edge arrays ----------------------------------------------------
     L.e_L.resize(E);
@@ -118,9 +115,9 @@ int build_layout(const fvgb_mesh_soa& m, const fvgb_params& p, Layout& L) {
             }
             g[6] = rx - m.elem_xy[r];
             g[7] = ry - m.elem_xy[(size_t)N + r];
-        } else {
-            g[6] = 0.0;
-            g[7] = 0.0;
+        } else {  // boundary edge: its midpoint (the double-Mach-reflection boundary tests it)
+            g[6] = fx;
+            g[7] = fy;
         }
     }
 

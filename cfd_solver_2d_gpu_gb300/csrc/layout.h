@@ -13,6 +13,7 @@ struct Layout {
     // edges (device order)
     std::vector<int> e_L, e_R, e_bc;
     std::vector<double> e_geom;      // [E][8]: nx, ny, length, 0, dLx, dLy, dRx, dRy
+                                     // (boundary edges: the midpoint x, y in place of dRx, dRy)
     // cells (device order)
     std::vector<int> c_edge;         // [N][3]: edge index, or ~index where the cell is R
     std::vector<int> c_nbr;          // [N][3]: valid face neighbours first, -1 after

@@ -61,6 +61,7 @@ struct RefMesh {  // device pointers, reference layout and numbering
     const int* edge_setID;
     const double* edge_length;
     const double* edge_normal;  // [2][E]
+    const double* edge_xy;      // [2][E] (read on "dsr" edges only)
     const int* boundary_type;   // [NB]
 };
 
@@ -72,7 +73,7 @@ __device__ __forceinline__ d4 load_ref(const double* U, int N, int c) {
 // reconstruction, on the reference's arrays; fluxes go to the file-scope array
 template <int FLUX>
 __global__ void __launch_bounds__(256) k_noalloc_flux(RefMesh m, const double* __restrict__ U, dev::Gas g,
-                                                      dev::BcData bc, double* __restrict__ F) {
+                                                      dev::BcData bc, double t_dsr, double* __restrict__ F) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m.E) return;
     const int L = m.edge_L[e], R = m.edge_R[e], set = m.edge_setID[e];
@@ -91,6 +92,11 @@ __global__ void __launch_bounds__(256) k_noalloc_flux(RefMesh m, const double* _
         dev::ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, uR);
     } else if (bt == 6013) {
         dev::ghost_farfield(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, uR);
+    } else if (bt == 6014) {
+        if (dev::dsr_upstream_at(m.edge_xy[e], m.edge_xy[(size_t)m.E + e], t_dsr, bc))
+            dev::ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, uR);
+        else
+            dev::ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, uR);
     } else if (R != -1) {  // interior and periodic edges: R holds the partner's cell
         uR = load_ref(U, m.N, R);
     }
@@ -151,14 +157,15 @@ extern "C" int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params
     m.edge_setID = dev_mesh->edge_setID;
     m.edge_length = dev_mesh->edge_length;
     m.edge_normal = dev_mesh->edge_normal;
+    m.edge_xy = dev_mesh->edge_xy;
     m.boundary_type = dev_mesh->boundary_type;
     const dev::Gas g = make_gas(*p);
     const dev::BcData bc = make_bc(*p);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (m.E > 0) {
         const int b = (m.E + 255) / 256;
-        if (p->flux_scheme == 2002) k_noalloc_flux<2002><<<b, 256, 0, s>>>(m, U_dev, g, bc, F);
-        else k_noalloc_flux<2001><<<b, 256, 0, s>>>(m, U_dev, g, bc, F);
+        if (p->flux_scheme == 2002) k_noalloc_flux<2002><<<b, 256, 0, s>>>(m, U_dev, g, bc, p->dsr_time, F);
+        else k_noalloc_flux<2001><<<b, 256, 0, s>>>(m, U_dev, g, bc, p->dsr_time, F);
     }
     if (m.N > 0) k_noalloc_gather<<<(m.N + 255) / 256, 256, 0, s>>>(m, F, rhs_dev);
     e = cudaGetLastError();

@@ -84,6 +84,10 @@ dev::BcData make_bc(const fvgb_params& p) {
     b.son_inlet = son(p.inlet);
     b.son_outlet = son(p.outlet);
     b.wall_ref = p.wall_bc_ref;
+    b.dsr_x = p.dsr[0];
+    b.sqrt3 = std::sqrt(3.0);  // CBoundaryDoubleShockReflect.cpp:7
+    b.clock_t0 = b.clock_dt = nullptr;
+    b.clock_frac = 0.0;
     return b;
 }
 
@@ -180,7 +184,7 @@ int Solver::init(const fvgb_mesh_soa& m, const fvgb_params& prm) {
     mv.dt_edge = d_dt_edge;
     // initial field (FieldInitializer) in the reference order, then on the device
     std::vector<double> U0((size_t)4 * N);
-    if (p.ic_type >= 1 && p.ic_type <= 3) {
+    if (p.ic_type >= 1 && p.ic_type <= 4) {
         rc = initial_field(m, p, U0.data());
         if (rc) return rc;
         rc = set_state(U0.data());
@@ -223,7 +227,11 @@ void Solver::enqueue_stage(int kind) {
         launches += 1;
     }
     mark(PROF_FLUX, true);
-    dev::launch_flux(s, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv, gas, bc, d_F,
+    dev::BcData b = bc;  // the stage's clock for the double-Mach-reflection boundary
+    b.clock_t0 = &d_state->t_old;
+    b.clock_dt = &d_state->dt;
+    b.clock_frac = dev::dsr_stage_frac(kind);
+    dev::launch_flux(s, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv, gas, b, d_F,
                      d_status, rec_tape.v ? &rec_tape : nullptr);
     mark(PROF_FLUX, false);
     launches += (mv.E_int > 0) + (mv.E > mv.E_int);
@@ -396,7 +404,11 @@ int Solver::rhs(const double* U, double* R, double* gx, double* gy) {
         dev::launch_grad(stream, p.gradient, p.limiter == 1, d_U, mv, d_Gx, d_Gy);
         launches += 1;
     }
-    dev::launch_flux(stream, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv, gas, bc,
+    dev::BcData b = bc;  // "dsr" edges at the handle's time t (the last step's end, or fvgb_step's t)
+    b.clock_t0 = &d_state->t;
+    b.clock_dt = &d_state->dt;
+    b.clock_frac = 0.0;
+    dev::launch_flux(stream, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv, gas, b,
                      d_F, d_status);
     dev::launch_update(stream, dev::STAGE_RHS, d_U, d_U0, d_K1, d_rhs, d_F, mv, d_state, gas, d_flags, d_flag_count,
                        kFlagCap, d_status);

@@ -24,6 +24,14 @@ __host__ __device__ constexpr bool final_stage(int kind) {
     return kind == STAGE_EULER || kind == STAGE_RK3_3 || kind == STAGE_SSP_3;
 }
 
+// The stage's time offset, in units of dt, at which the double-Mach-reflection boundary is
+// evaluated: CIteration.cpp:61-62 set its clock to (t, 0) for the step, and
+// evolve_rk3_globaltimestep (Evolve.cpp:43-77) sets dt, then 0.5 dt, before its second and
+// third residuals.  SSP-RK3's stages sit at t, t + dt and t + dt/2 as well.
+__host__ __device__ constexpr double dsr_stage_frac(int kind) {
+    return (kind == STAGE_RK3_2 || kind == STAGE_SSP_2) ? 1.0 : (kind == STAGE_RK3_3 || kind == STAGE_SSP_3) ? 0.5 : 0.0;
+}
+
 // ---- time step ---------------------------------------------------------------
 
 // update_host_ruvp_Uold, FVMR/src/time/CIteration.cpp:163-180 (plus U0 <- U)
@@ -360,7 +368,21 @@ __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, c
     F[e] = flux;
 }
 
-// a boundary edge with a ghost state (walls, far field, inlet, outlet, symmetry); with REC
+// The double-Mach-reflection boundary (Flux.cpp:21-26 and 280-287): the edge is upstream of
+// the shock when its midpoint lies left of shock_x + (y + 20 t) / sqrt(3)
+// (CBoundaryDoubleShockReflect::isUpStreamOfShock_atBoundary, CBoundaryDoubleShockReflect.cpp:
+// 36-49, shock speed 20 from CBoundaryDoubleShockReflect.h:15), t being the stage's time
+// get_t_plus_dt(); rounded operation by operation, without contraction, as the reference.
+__device__ __forceinline__ bool dsr_upstream_at(double x, double y, double t, const BcData& bc) {
+    const double right = __dadd_rn(bc.dsr_x, __ddiv_rn(__dadd_rn(y, __dmul_rn(20.0, t)), bc.sqrt3));
+    return x < right;
+}
+__device__ __forceinline__ bool dsr_upstream(double x, double y, const BcData& bc) {
+    return dsr_upstream_at(x, y, __dadd_rn(*bc.clock_t0, __dmul_rn(bc.clock_frac, *bc.clock_dt)), bc);
+}
+
+// a boundary edge with a ghost state (walls, far field, inlet, outlet, symmetry,
+// double Mach reflection); with REC
 // (Roe, Euler) the tape entry of slip-wall and symmetry edges is written as well
 template <int FLUX, bool LINEAR, bool NS, bool REC = false>
 __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, const d4* __restrict__ Gx,
@@ -410,6 +432,13 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
     case 6013:
         if (!ghost_farfield(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
         break;
+    case 6014: {  // boundary edges keep their midpoint in the slots of the absent R offset
+        const bool up = dsr_upstream(__ldg(&gm[6]), __ldg(&gm[7]), bc);
+        const bool ok = up ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
+                           : ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR);
+        if (!ok) atomicAdd(&st->farfield_oor, 1ull);
+        break;
+    }
     default:
         break;
     }

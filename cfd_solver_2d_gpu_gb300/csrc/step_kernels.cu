@@ -52,6 +52,7 @@ __global__ void k_dt_final(StepState* s, int advance) {
     s->dt_raw = dt;
     if (advance) {
         if (s->t + dt > s->T) dt = s->T - s->t;
+        s->t_old = s->t;
         s->t += dt;
         s->dt = dt;
         s->dt6 = dt / 6.0;

@@ -12,6 +12,7 @@ namespace dev {
 struct StepState {
     double t, T, dt, dt6, dt_raw;
     unsigned long long dtmin_bits;
+    double t_old;  // t at the start of the step (the clock of the double-Mach-reflection boundary)
 };
 
 void launch_prim(cudaStream_t s, const d4* U, d4* U0, d4* prim, int N, const Gas& g, bool copy);

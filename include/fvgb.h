@@ -45,17 +45,25 @@ typedef struct fvgb_params {
     int lsq_det_ref;     /* [gpu] lsq_det = "ref" (1) keeps MatrixKernel.h:48-49, "fixed" (0) corrects it */
     int wall_bc_ref;     /* [gpu] wall_bc = "ref" (1) keeps Flux.cpp:73-79, "mirror" (0) mirrors the velocity */
     int restrict_ref;    /* [gpu] restrict = "ref" (1) keeps Restrict.cpp:52, "fixed" (0) corrects it */
-    int ic_type;         /* initialCondition.type: 1 uniform, 2 isentropic vortex, 3 shock tube */
+    int ic_type;         /* initialCondition.type: 1 uniform, 2 isentropic vortex, 3 shock tube,
+                            4 double Mach reflection */
     int renumber;        /* [gpu] renumber: 0 keep the file order, 1 Morton order of cells and edges */
     int device;          /* CUDA device ordinal */
     double gamma, R, Pr, mu0, T0, CFL, T_end, Re;
     double inf[4], inlet[4], outlet[4];   /* rho, u, v, p */
     double vortex[3];    /* x, y, strength */
-    double shock[4];     /* shock tube: x, y, normal x, normal y */
+    double shock[4];     /* shock tube: x, y, normal x, normal y (defaults 0, 0, 1, 0) */
     double mesh_scale;   /* constant.mesh_scale_factor */
     int max_iteration;   /* output.maxIteration */
     int pad_;
     double ref_area;     /* constant.referenceArea x mesh_scale_factor (TomlFileManager.cpp:128-131) */
+    /* double Mach reflection (initialCondition.doubleShockReflection, FieldInitializer.cpp:93-108):
+     * where the shock meets the wall (x, y) and its angle in degrees, [0, 90] */
+    double dsr[3];
+    /* the time at which fvgb_rhs_noalloc evaluates "dsr" boundary edges (it has no clock of its
+     * own; the reference reads CBoundaryDoubleShockReflect's t + dt there, Flux.cpp:328-332).
+     * The handle-based entry points keep their own clock and ignore it. */
+    double dsr_time;
 } fvgb_params;
 
 /* Reference-order mesh arrays, mirroring GPU::NodeSoA / ElementSoA / EdgeSoA /
@@ -292,7 +300,8 @@ int fvgb_batch_info(fvgb_batch* b, long long out[8]);
  * device or pinned memory: for callers that already manage every GPU buffer
  * themselves and may not add allocations of their own.  dev_mesh holds DEVICE
  * pointers to the reference-layout arrays (elem_edges, elem_volume, edge_L,
- * edge_R, edge_setID, edge_length, edge_normal, boundary_type are read);
+ * edge_R, edge_setID, edge_length, edge_normal, boundary_type are read, and
+ * edge_xy where a "dsr" boundary exists: its edges are evaluated at p->dsr_time);
  * U_dev is U[4][N] and rhs_dev receives RHS[4][N] = -(1/vol) sum of edge
  * fluxes, both on the device; stream is a cudaStream_t (NULL = default
  * stream); the call only enqueues work.  The edge fluxes are kept in one

@@ -524,6 +524,38 @@ int om_init_field(const om_mesh* m, const om_params* p, int ic, const double* vo
         }
         return 0;
     }
+    if (ic == 3) { /* FieldInitializer::setInitialShockTube, FieldInitializer.cpp:179-222 */
+        double sx = p->shock[0], sy = p->shock[1], snx = p->shock[2], sny = p->shock[3];
+        if (snx == 0.0 && sny == 0.0) snx = 1.0;
+        double length_inv = 1.0 / sqrt(snx * snx + sny * sny);
+        snx *= length_inv;
+        sny *= length_inv;
+        double ui[4], uo[4];
+        ruvp2U(p->inlet, ui, gamma);
+        ruvp2U(p->outlet, uo, gamma);
+        for (int e = 0; e < N; e++) {
+            double x = m->elem_xy[e], y = m->elem_xy[N + e];
+            int inlet;
+            if (snx == 1.0) inlet = x < sx;
+            else inlet = !((x - sx) * snx + (y - sy) * sny > 0);
+            for (int j = 0; j < 4; j++) U[j * N + e] = inlet ? ui[j] : uo[j];
+        }
+        return 0;
+    }
+    if (ic == 4) { /* FieldInitializer::setInitialDoubleShockReflection, FieldInitializer.cpp:224-260,
+                      with isUpStreamOfShock_forElement, CBoundaryDoubleShockReflect.cpp:17-33 */
+        double angle_rad = p->dsr[2] * OM_PI / 180.0;
+        double norm_x = -sin(angle_rad), norm_y = cos(angle_rad);
+        double ui[4], uo[4];
+        ruvp2U(p->inlet, ui, gamma);
+        ruvp2U(p->outlet, uo, gamma);
+        for (int e = 0; e < N; e++) {
+            double r_x = m->elem_xy[e] - p->dsr[0], r_y = m->elem_xy[N + e] - p->dsr[1];
+            int up = r_x * norm_x + r_y * norm_y > 0;
+            for (int j = 0; j < 4; j++) U[j * N + e] = up ? ui[j] : uo[j];
+        }
+        return 0;
+    }
     return -1;
 }
 
@@ -863,8 +895,13 @@ static int edge_flux(const om_mesh* m, const om_params* p, const double* U, cons
     case BC_INF:
         if (ghost_farfield(UL, p->inf, UR, nx, ny, p->gamma)) return -4;
         break;
-    case BC_DSR:
-        return -5; /* double-Mach-reflection boundary: not part of this path */
+    case BC_DSR: { /* Flux.cpp:280-287 with isUpStreamOfShock_atBoundary_static_inline (Flux.cpp:21-26):
+                      shock speed 20 (CBoundaryDoubleShockReflect.h:15), sqrt3 = sqrt(3.0) */
+        double right = p->dsr[0] + (y + 20.0 * p->dsr_time) / sqrt(3.0);
+        const double* far = (x < right) ? p->inlet : p->outlet;
+        if (ghost_farfield(UL, far, UR, nx, ny, p->gamma)) return -4;
+        break;
+    }
     default:
         if (R != -1) {
             if (setID != -1) { /* periodic: reconstruct R at the partner edge's midpoint */
@@ -1084,37 +1121,46 @@ int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* 
     double *k2 = (double*)malloc(M * sizeof(double)), *k3 = (double*)malloc(M * sizeof(double));
     double *Us = (double*)malloc(M * sizeof(double)), *U1 = (double*)malloc(M * sizeof(double));
     int rc = 0;
+    om_params ps = *p; /* ps.dsr_time: the stage's clock, CIteration.cpp:60-62 and Evolve.cpp:43-77 */
     for (int s = 0; s < nsteps; s++) {
         double dt;
         rc = om_dt(m, p, U, &dt, NULL);
         if (rc) break;
         if (*t + dt > p->T_end) dt = p->T_end - *t; /* CIteration.cpp:59 */
+        const double t0 = *t;
         *t += dt;
         if (dts) dts[s] = dt;
         memcpy(U0, U, M * sizeof(double));
         if (p->time_advance == 3101) { /* evolve_explicit_globaltimestep, Evolve.cpp:12-23 */
-            if ((rc = om_rhs(m, p, U0, k1, NULL, NULL))) break;
+            ps.dsr_time = t0 + 0.0;
+            if ((rc = om_rhs(m, &ps, U0, k1, NULL, NULL))) break;
             #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) U[i] = U0[i] + dt * k1[i];
         } else if (p->time_advance == 3103) { /* Kutta RK3 with the weights of Evolve.cpp:58-86 */
-            if ((rc = om_rhs(m, p, U0, k1, NULL, NULL))) break;
+            ps.dsr_time = t0 + 0.0;
+            if ((rc = om_rhs(m, &ps, U0, k1, NULL, NULL))) break;
             #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) Us[i] = U0[i] + 0.5 * dt * k1[i];
-            if ((rc = om_rhs(m, p, Us, k2, NULL, NULL))) break;
+            ps.dsr_time = t0 + dt;
+            if ((rc = om_rhs(m, &ps, Us, k2, NULL, NULL))) break;
             #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) Us[i] = U0[i] - dt * k1[i] + 2.0 * dt * k2[i];
-            if ((rc = om_rhs(m, p, Us, k3, NULL, NULL))) break;
+            ps.dsr_time = t0 + 0.5 * dt;
+            if ((rc = om_rhs(m, &ps, Us, k3, NULL, NULL))) break;
             const double dt_on_6 = dt / 6.0;
             #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) U[i] = U0[i] + dt_on_6 * (k1[i] + 4 * k2[i] + k3[i]);
         } else if (p->time_advance == 3104) { /* SSP-RK3 (Shu-Osher), new in this path */
-            if ((rc = om_rhs(m, p, U0, k1, NULL, NULL))) break;
+            ps.dsr_time = t0 + 0.0;
+            if ((rc = om_rhs(m, &ps, U0, k1, NULL, NULL))) break;
             #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) U1[i] = U0[i] + dt * k1[i];
-            if ((rc = om_rhs(m, p, U1, k2, NULL, NULL))) break;
+            ps.dsr_time = t0 + dt;
+            if ((rc = om_rhs(m, &ps, U1, k2, NULL, NULL))) break;
             #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) Us[i] = 0.75 * U0[i] + 0.25 * (U1[i] + dt * k2[i]);
-            if ((rc = om_rhs(m, p, Us, k3, NULL, NULL))) break;
+            ps.dsr_time = t0 + 0.5 * dt;
+            if ((rc = om_rhs(m, &ps, Us, k3, NULL, NULL))) break;
             #pragma omp parallel for schedule(static)
             for (size_t i = 0; i < M; i++) U[i] = (1.0 / 3.0) * U0[i] + (2.0 / 3.0) * (Us[i] + dt * k3[i]);
         } else {

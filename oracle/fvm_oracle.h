@@ -47,6 +47,9 @@ typedef struct om_params {
     int pad_;
     double gamma, R, Pr, mu0, T0, CFL, T_end;
     double inf[4], inlet[4], outlet[4]; /* rho, u, v, p */
+    double shock[4];   /* shock tube: x, y, normal x, normal y */
+    double dsr[3];     /* double Mach reflection: x, y where the shock meets the wall, angle (degrees) */
+    double dsr_time;   /* CBoundaryDoubleShockReflect's t + dt: the time of "dsr" edges in om_rhs */
 } om_params;
 
 /* Reads an .su2 file and assembles the mesh exactly as the reference does.
@@ -54,7 +57,8 @@ typedef struct om_params {
 om_mesh* om_mesh_read_su2(const char* path, int equation, double scale, char* err, int errlen);
 void om_mesh_free(om_mesh* m);
 
-/* Initial field: ic 1 uniform (inf), 2 isentropic vortex (vortex = x, y, strength). */
+/* Initial field: ic 1 uniform (inf), 2 isentropic vortex (vortex = x, y, strength),
+ * 3 shock tube (params shock), 4 double Mach reflection (params dsr). */
 int om_init_field(const om_mesh* m, const om_params* p, int ic, const double* vortex, double* U);
 /* One residual evaluation: RHS = -(1/vol) * sum of edge fluxes; also the limited gradients. */
 int om_rhs(const om_mesh* m, const om_params* p, const double* U, double* rhs, double* gx, double* gy);
@@ -62,7 +66,8 @@ int om_rhs(const om_mesh* m, const om_params* p, const double* U, double* rhs, d
 int om_dt(const om_mesh* m, const om_params* p, const double* U, double* dt, double* alpha);
 /* Positivity pass on U in place. Returns the number of cells replaced, -1 on NaN. */
 int om_restrict(const om_mesh* m, const om_params* p, double* U);
-/* nsteps steps of time_advance from time *t; U in place; dts[nsteps] may be NULL. */
+/* nsteps steps of time_advance from time *t; U in place; dts[nsteps] may be NULL.
+ * "dsr" edges are evaluated at each stage's time (p->dsr_time is not used). */
 int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* t, double* dts, double* last_rhs);
 /* Residual norm of an RHS field: norm 0 = L-infinity, 1 = L1, 2 = L2 (per variable). */
 void om_residual(const om_mesh* m, const double* rhs, int norm, double* out4);

@@ -34,7 +34,8 @@ class OmParams(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("equation", "flux_scheme", "reconstruct", "gradient", "limiter",
                                            "time_advance", "lsq_det_ref", "wall_bc_ref", "restrict_ref", "pad_")] + [
         (n, ctypes.c_double) for n in ("gamma", "R", "Pr", "mu0", "T0", "CFL", "T_end")] + [
-        ("inf", ctypes.c_double * 4), ("inlet", ctypes.c_double * 4), ("outlet", ctypes.c_double * 4)]
+        ("inf", ctypes.c_double * 4), ("inlet", ctypes.c_double * 4), ("outlet", ctypes.c_double * 4),
+        ("shock", ctypes.c_double * 4), ("dsr", ctypes.c_double * 3), ("dsr_time", ctypes.c_double)]
 
 
 def build():
@@ -189,6 +190,15 @@ def params_from_toml(cfg):
     p.limiter = int(g("inviscid_flux_method.flux_limiter", 2))
     for key, field in _QUIRK_KEYS.items():
         setattr(p, field, 1 if str(g(f"gpu.{key}", "ref")) == "ref" else 0)
+    # FieldInitializer::initialize_using_config (FieldInitializer.cpp:74-110), defaults of
+    # FieldInitializer.h:23-26 and CBoundaryDoubleShockReflect.h:12-14
+    p.shock[:] = [float(g(f"initialCondition.shockTube.{k}", d)) for k, d in
+                  (("shock_x", 0.0), ("shock_y", 0.0), ("shock_normal_x", 1.0), ("shock_normal_y", 0.0))]
+    if ic_type == 4:
+        p.dsr[:] = [float(g(f"initialCondition.doubleShockReflection.{k}")) for k in
+                    ("shock_x", "shock_y", "shock_angle_degree")]
+    else:
+        p.dsr[:] = [0.0, 0.0, 60.0]
     info = {"ic_type": ic_type, "mesh_scale": float(g("constant.mesh_scale_factor", 1.0)),
             "vortex": [float(g("initialCondition.isentropicVortex.vortex_x", 0.0)),
                        float(g("initialCondition.isentropicVortex.vortex_y", 0.0)),

@@ -13,7 +13,9 @@
 //              reference's RK3 exactly as written (Evolve.cpp:25-96)
 //   rk3        classical (Kutta) RK3 with the weights of Evolve.cpp:26-37,
 //              each stage evaluated by the reference's calculateFunctionF on
-//              the solver singleton (Evolve.cpp:98-112)
+//              the solver singleton (Evolve.cpp:98-112), the double-Mach-
+//              reflection clock set as CIteration.cpp:60-62 and Evolve.cpp:43-77
+//              set it (t; then dt 0, dt, 0.5 dt for the three stages)
 //   ssprk3     Shu-Osher SSP-RK3 built the same way (new code 3104)
 //   rhs        one calculateFunctionF on the initial field, plus its dt
 //   mesh       assembly and initial field only
@@ -209,6 +211,9 @@ int main(int argc, char** argv) {
         }
         myfloat dt = global_dt(s);
         if (t + dt > T) dt = T - t;
+        CBoundaryDoubleShockReflect* dsr = CBoundaryDoubleShockReflect::getInstance();
+        dsr->set_t(t);
+        dsr->set_dt(0.0);
         t += dt;
         dts.push_back((double)dt);
         copy_field(s.elementField_host.U, U0, N);
@@ -218,9 +223,11 @@ int main(int argc, char** argv) {
             // weights and stage points of FVMR/src/time/Evolve.cpp:58-86
             residual(s, U0, k1);
             for (size_t i = 0; i < M; i++) Us[i] = (double)((myfloat)U0[i] + 0.5 * dt * (myfloat)k1[i]);
+            dsr->set_dt(dt);
             residual(s, Us, k2);
             for (size_t i = 0; i < M; i++)
                 Us[i] = (double)((myfloat)U0[i] - dt * (myfloat)k1[i] + 2.0 * dt * (myfloat)k2[i]);
+            dsr->set_dt(0.5 * dt);
             residual(s, Us, k3);
             const myfloat dt_on_6 = dt / 6.0;
             for (size_t i = 0; i < M; i++)
@@ -231,9 +238,11 @@ int main(int argc, char** argv) {
             residual(s, U0, k1);
             std::vector<double> U1(M), U2(M);
             for (size_t i = 0; i < M; i++) U1[i] = (double)((myfloat)U0[i] + dt * (myfloat)k1[i]);
+            dsr->set_dt(dt);
             residual(s, U1, k2);
             for (size_t i = 0; i < M; i++)
                 U2[i] = (double)(0.75 * (myfloat)U0[i] + 0.25 * ((myfloat)U1[i] + dt * (myfloat)k2[i]));
+            dsr->set_dt(0.5 * dt);
             residual(s, U2, k3);
             for (size_t i = 0; i < M; i++)
                 Us[i] = (double)((1.0 / 3.0) * (myfloat)U0[i] + (2.0 / 3.0) * ((myfloat)U2[i] + dt * (myfloat)k3[i]));

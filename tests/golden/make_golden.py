@@ -41,7 +41,13 @@ def golden_cases(d):
     sq64 = cases.square_mesh(64, directory=d)
     cyl = cases.cylinder_mesh(32, 16, directory=d)
     ch24j = cases.channel_mesh(24, jitter=0.2, directory=d)
+    dmr48 = cases.dmr_mesh(48, jitter=0.2, directory=d)
     T = cases.toml_text
+    # the double Mach reflection of the reference's own example (2D_double_shock_reflect/input.toml):
+    # shock at (1/6, 0), 60 degrees; post-shock inlet (8, 8.25 at -30 degrees, 116.5), still gas ahead
+    dmr = dict(ic_type=4, dmr=(1.0 / 6.0, 0.0, 60.0), inlet=(8.0, 8.25, -30.0, 116.5, "angle"),
+               outlet=(1.4, 0.0, 0.0, 1.0, "angle"))
+    sod = dict(ic_type=3, inlet=(1.0, 0.0, 0.0, 1.0), outlet=(0.125, 0.0, 0.0, 0.1))
     return [
         # the small plain config: 64x64 vortex, Roe, first order, Kutta RK3, CFL 0.5, 1000 steps
         ("vortex64_roe_o1_rk3", T(flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=3103, CFL=0.5),
@@ -83,6 +89,21 @@ def golden_cases(d):
                                          time_advance=3103, CFL=0.5, vortex=(5.0, 2.5, 5.0), inf=(1.0, 1.0, 0.3, 1.0),
                                          Re=100.0, inlet=(1.0, 1.0, 0.3, 1.0), outlet=(1.0, 1.0, 0.0, 0.9)),
          ch24j, "rk3", 5),
+        # double Mach reflection: the "dsr" edges switch from the inlet to the outlet state where the
+        # moving shock crosses the top boundary, at each stage's time; the runs are long enough
+        # (t > 0.0042) for the crossing to pass one edge midpoint
+        ("dmr48_roe_gg_barth_euler", T(flux=2002, reconstruct=3002, gradient=2, limiter=1, time_advance=3101,
+                                       CFL=0.5, **dmr), dmr48, "euler", 40),
+        ("dmr48_llf_lsq_barth_ssp", T(flux=2001, reconstruct=3002, gradient=1, limiter=1, time_advance=3104,
+                                      CFL=0.5, **dmr), dmr48, "ssprk3", 25),
+        ("dmr48_ns_lsq_barth_rk3", T(equation=2, flux=2002, reconstruct=3002, gradient=1, limiter=1,
+                                     time_advance=3103, CFL=0.5, Re=1000.0, **dmr), dmr48, "rk3", 25),
+        # shock tubes (Sod states): the normal along +x, and a tilted one
+        ("sod_channel24_roe_o1_rk3", T(flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=3103,
+                                       CFL=0.5, shock_tube=(5.0, 0.0, 1.0, 0.0), **sod), ch24j, "rk3", 20),
+        ("sod_tilted_channel24_llf_lsq_barth_ssp", T(flux=2001, reconstruct=3002, gradient=1, limiter=1,
+                                                     time_advance=3104, CFL=0.5, shock_tube=(5.0, 5.0, 0.6, 0.8),
+                                                     **sod), ch24j, "ssprk3", 10),
     ]
 
 

@@ -79,6 +79,25 @@ def test_batch_matches_plain_channels(tmp_path):
         assert t[i] == tp
 
 
+def test_batch_matches_plain_double_mach_reflection(tmp_path):
+    """"dsr" edges on each instance's own clock, evaluated at each stage's time: the runs
+    are long enough for the shock to pass an edge midpoint on the top boundary."""
+    inst = []
+    for i, (n, cfl) in enumerate(((24, 0.4), (48, 0.5), (24, 0.3))):
+        tp, sp = cases.write_case(str(tmp_path), f"dmr{i}", cases.toml_text(
+            flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3103, CFL=cfl, ic_type=4,
+            dmr=(1.0 / 6.0, 0.0, 60.0), inlet=(8.0, 8.25, -30.0, 116.5, "angle"), outlet=(1.4, 0.0, 0.0, 1.0)),
+            cases.dmr_mesh(n, jitter=0.2, directory=str(tmp_path)))
+        inst.append(load(tp, sp))
+    b = fv.Batch([m for m, _ in inst], [p for _, p in inst])
+    t = b.step(25)
+    assert t[1] > 0.0042  # past the crossing of the 48-cell instance's tenth top edge
+    for i, (m, p) in enumerate(inst):
+        U, tp = plain_run(m, p, 25)
+        assert np.array_equal(b.get_state(i), U), i
+        assert t[i] == tp
+
+
 def test_autotuner_keeps_state_and_result(tmp_path):
     inst = cylinders(tmp_path, [8, 14, 5], [0.1, 0.4, 0.6])
     b = fv.Batch([m for m, _ in inst], [p for _, p in inst])

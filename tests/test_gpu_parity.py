@@ -3,7 +3,8 @@ golden fixtures the reference produced, against the oracle on the same inputs
 at larger sizes, and through size-independent properties at full size.
 
 Tolerances are relative L-infinity norms, ||a - b||_inf / ||b||_inf, in FP64:
-  residual, gradients, dt of one evaluation     1e-12
+  residual, gradients, dt of one evaluation     1e-12 (gradients: relative to the
+                                                larger of ||b||_inf and max|U| / h)
   state after <= 20 steps                       1e-12
   state after 1000 steps (64x64 vortex)         1e-9
   second-order limited runs (<= 10 steps)       1e-10
@@ -24,6 +25,15 @@ def rel(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
+def rel_grad(a, b, U, vol):
+    """Gradients relative to the larger of their own maximum and the field's scale
+    max|U| / sqrt(mean cell area): where every gradient is limited away or the field is
+    piecewise uniform, both sides hold round-off alone (the reference's Green-Gauss sums
+    leave ~1e-14 where this library's give exact zeros)."""
+    scale = max(np.max(np.abs(b)), np.max(np.abs(U)) / np.sqrt(np.mean(vol)))
+    return float(np.max(np.abs(a - b)) / scale)
+
+
 def make(tp, sp, renumber=1):
     p = fv.Params.from_toml(tp)
     p.renumber = renumber
@@ -42,7 +52,8 @@ def test_residual_matches_reference(golden):
     R, gx, gy = s.rhs(g["U0"], gradients=True)
     assert rel(R, g["rhs"]) <= 1e-12, name
     if p.reconstruct == 3002 or p.equation == 2:
-        assert rel(gx, g["grad_x"]) <= 1e-12 and rel(gy, g["grad_y"]) <= 1e-12, name
+        assert rel_grad(gx, g["grad_x"], g["U0"], g["elem_vol"]) <= 1e-12, name
+        assert rel_grad(gy, g["grad_y"], g["U0"], g["elem_vol"]) <= 1e-12, name
     s.set_state(g["U0"])
     assert abs(s.dt() - g["dt"][0]) <= 1e-12 * g["dt"][0], name
 

@@ -140,3 +140,39 @@ def test_channel_boundaries_and_inlet_tables(tmp_path):
     # (Ma, AoA) with T0, p0 the stagnation state: flow at 10 degrees, static pressure below p0
     assert np.degrees(np.arctan2(p.inlet[2], p.inlet[1])) == pytest.approx(10.0, rel=1e-12)
     assert p.inlet[3] < 101325.0
+
+
+def test_double_mach_reflection_and_shock_tube_inputs(tmp_path):
+    """[initialCondition.doubleShockReflection] is required for type 4 and its angle must lie in
+    [0, 90] (FieldInitializer.cpp:93-105); the shock tube's normal defaults to +x
+    (FieldInitializer.h:23-26); both initial fields equal the oracle's."""
+    from oracle.pyoracle import Oracle
+    dmr = dict(ic_type=4, inlet=(8.0, 8.25, -30.0, 116.5, "angle"), outlet=(1.4, 0.0, 0.0, 1.0))
+    tp = tmp_path / "dmr.toml"
+    tp.write_text(cases.toml_text(**dmr))
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Params.from_toml(str(tp))
+    assert e.value.code == -3 and "doubleShockReflection" in str(e.value)
+    tp.write_text(cases.toml_text(dmr=(0.2, 0.0, 95.0), **dmr))
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Params.from_toml(str(tp))
+    assert "shock_angle_degree" in str(e.value)
+    sp = cases.dmr_mesh(24, jitter=0.2, directory=str(tmp_path))
+    for angle in (60.0, 90.0, 35.0):
+        tp.write_text(cases.toml_text(dmr=(1.0 / 6.0, 0.0, angle), **dmr))
+        p = fv.Params.from_toml(str(tp))
+        U = fv.initial_field(fv.Mesh.read_su2(sp, p), p)
+        assert np.array_equal(U, Oracle(str(tp), sp).init_field()), angle
+        assert 0 < np.count_nonzero(U[0] == 8.0) < U.shape[1]
+    sod = dict(ic_type=3, inlet=(1.0, 0.0, 0.0, 1.0), outlet=(0.125, 0.0, 0.0, 0.1))
+    sp = cases.channel_mesh(12, jitter=0.2, directory=str(tmp_path))
+    for shock in (None, (4.0, 0.0, 0.0, 0.0), (5.0, 5.0, -0.6, 0.8)):
+        tp.write_text(cases.toml_text(shock_tube=shock, **sod))
+        p = fv.Params.from_toml(str(tp))
+        U = fv.initial_field(fv.Mesh.read_su2(sp, p), p)
+        assert np.array_equal(U, Oracle(str(tp), sp).init_field()), shock
+    tp.write_text(cases.toml_text(**sod))
+    p = fv.Params.from_toml(str(tp))
+    assert list(p.shock) == [0.0, 0.0, 1.0, 0.0]
+    U = fv.initial_field(fv.Mesh.read_su2(sp, p), p)
+    assert np.all(U[0] == 0.125)  # every centroid lies at x > 0: downstream of the default shock

@@ -38,7 +38,7 @@ def device_mesh(mesh):
     return soa, keep
 
 
-@pytest.mark.parametrize("kind", ["vortex_roe", "cylinder_llf"])
+@pytest.mark.parametrize("kind", ["vortex_roe", "cylinder_llf", "dmr_roe"])
 def test_rhs_noalloc_matches_rhs(tmp_path, kind):
     import torch
     L = fv.lib()
@@ -47,17 +47,26 @@ def test_rhs_noalloc_matches_rhs(tmp_path, kind):
                                    ctypes.c_void_p]
     if kind == "vortex_roe":
         tp, su2 = cases.vortex_small(str(tmp_path), n=64)
-    else:
+    elif kind == "cylinder_llf":
         tp = str(tmp_path / "cyl.toml")
         with open(tp, "w") as f:
             f.write(cases.toml_text(equation=1, flux=2001, reconstruct=3001, gradient=1, limiter=1,
                                     time_advance=3103, CFL=0.5, ic_type=1, inf_mode=0, Ma=0.5))
         su2 = cases.cylinder_mesh(64, 32, directory=str(tmp_path))
+    else:  # double Mach reflection: "dsr" edges at p.dsr_time against the handle's clock
+        tp = str(tmp_path / "dmr.toml")
+        with open(tp, "w") as f:
+            f.write(cases.toml_text(equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1,
+                                    time_advance=3101, CFL=0.5, ic_type=4, dmr=(1.0 / 6.0, 0.0, 60.0),
+                                    inlet=(8.0, 8.25, -30.0, 116.5, "angle"), outlet=(1.4, 0.0, 0.0, 1.0)))
+        su2 = cases.dmr_mesh(48, jitter=0.2, directory=str(tmp_path))
     p = fv.Params.from_toml(tp)
     mesh = fv.Mesh.read_su2(su2, p)
     solver = fv.GPUSolver2(mesh, p)
     U0 = solver.get_state()
-    solver.step(0.0, p.T_end, 3)
+    # the DMR run starts just before the shock reaches the tenth top edge's midpoint (t = 0.00413)
+    t = solver.step(0.0041 if kind == "dmr_roe" else 0.0, p.T_end, 3)
+    p.dsr_time = t  # the handle's clock after the steps
     U1 = solver.get_state()
     soa, keep = device_mesh(mesh)
     stream = torch.cuda.current_stream().cuda_stream
@@ -69,6 +78,12 @@ def test_rhs_noalloc_matches_rhs(tmp_path, kind):
         torch.cuda.synchronize()
         ref = solver.rhs(U)
         assert rel(Rd.cpu().numpy(), ref) <= 1e-12
+    if kind == "dmr_roe":  # the time matters: at t = 0 the tenth top edge is still downstream (outlet state)
+        p.dsr_time = 0.0
+        rc = L.fvgb_rhs_noalloc(ctypes.byref(soa), ctypes.addressof(p), Ud.data_ptr(), Rd.data_ptr(), stream)
+        assert rc == 0
+        torch.cuda.synchronize()
+        assert rel(Rd.cpu().numpy(), ref) > 1e-6
 
 
 def test_rhs_noalloc_rejects_what_it_cannot_hold():
