@@ -39,7 +39,8 @@ class Params(ctypes.Structure):
         ("inf", ctypes.c_double * 4), ("inlet", ctypes.c_double * 4), ("outlet", ctypes.c_double * 4),
         ("vortex", ctypes.c_double * 3), ("shock", ctypes.c_double * 4), ("mesh_scale", ctypes.c_double),
         ("max_iteration", ctypes.c_int), ("pad_", ctypes.c_int), ("ref_area", ctypes.c_double),
-        ("dsr", ctypes.c_double * 3), ("dsr_time", ctypes.c_double)]
+        ("dsr", ctypes.c_double * 3), ("dsr_time", ctypes.c_double), ("steady", ctypes.c_int),
+        ("pad2_", ctypes.c_int), ("CFL_steady", ctypes.c_double)]
 
     @classmethod
     def default(cls):

@@ -29,7 +29,8 @@ def _num(x):
 def toml_text(*, equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=3103, CFL=0.5,
               T_end=1000.0, ic_type=2, vortex=(5.0, 5.0, 5.0), inf_mode=1, inf=(1.0, 1.0, 1.0, 1.0), Ma=0.2,
               AoA=0.0, Re=None, mu0=17.9e-6, Pr=0.72, ref_area=1.0, lsq_det="ref", wall_bc="ref", restrict="ref",
-              renumber=1, filename="mesh", max_iteration=1000, inlet=None, outlet=None, shock_tube=None, dmr=None):
+              renumber=1, filename="mesh", max_iteration=1000, inlet=None, outlet=None, shock_tube=None, dmr=None,
+              steady=False, CFL_steady=0.8):
     """inlet / outlet: None (table left out, the reference's default state), (rho, u, v, p)
     (input_mode 1), (rho, u, angle_degree, p, "angle") (input_mode 3) or (Ma, AoA)
     (input_mode 0), as [boundaryCondition.2D.inlet|outlet].  shock_tube: (x, y, normal x,
@@ -72,7 +73,9 @@ def toml_text(*, equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1,
     lines += ["", "[output]", "step_per_print = 50", "step_per_output_field = 100", "step_per_output_hist = 100",
               f"maxIteration = {max_iteration}", "tolerace_residual = 1e-7", "",
               "[physicsModel]", f"equation = {equation}", "",
-              "[time]", "is_steady = 0", "is_explicit = 1", f"CFL = {_num(CFL)}", f"max_physical_time = {_num(T_end)}",
+              "[time]", f"is_steady = {1 if steady else 0}", "is_explicit = 1"] + (
+                  [f"CFL = {_num(CFL)}"] if CFL is not None else []) + [
+              f"CFL_steady = {_num(CFL_steady)}", f"max_physical_time = {_num(T_end)}",
               f"time_advance = {time_advance}", "",
               "[inviscid_flux_method]", f"flag_reconstruct = {reconstruct}", f"flag_gradient = {gradient}",
               f"flux_conservation_scheme = {flux}", f"flux_limiter = {limiter}", "",

@@ -381,6 +381,7 @@ struct Adjoint {
         s = solver;
         const fvgb_params& p = s->p;
         if (p.equation != 1) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers the Euler equations");
+        if (p.steady) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers time-accurate runs (time.is_steady = 0)");
         if (p.flux_scheme != 2002) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers the Roe flux");
         if (p.time_advance != 3101 && p.time_advance != 3104)
             return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers forward Euler (3101) and SSP-RK3 (3104)");

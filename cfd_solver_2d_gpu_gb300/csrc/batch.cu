@@ -293,6 +293,9 @@ struct Batch {
                 return fail(FVGB_ERR_ARG, "batched instances must share the scheme and the gas constants");
         }
         if (p.equation != 1) return fail(FVGB_ERR_UNSUPPORTED, "the batched form runs the Euler equations");
+        for (int i = 0; i < n; i++)
+            if (params[i].steady)
+                return fail(FVGB_ERR_UNSUPPORTED, "the batched form steps in time (time.is_steady = 0)");
         if (p.time_advance != 3101 && p.time_advance != 3103 && p.time_advance != 3104)
             return fail(FVGB_ERR_ARG, "invalid time_advance");
         BK(cudaSetDevice(p.device));

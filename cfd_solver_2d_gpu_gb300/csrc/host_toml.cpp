@@ -247,6 +247,7 @@ extern "C" int fvgb_params_default(fvgb_params* p) {
     p->vortex[2] = 1;
     p->shock[2] = 1.0;  // FieldInitializer.h:23-26: the shock normal points along +x
     p->dsr[2] = 60.0;   // CBoundaryDoubleShockReflect.h:14
+    p->CFL_steady = 0.95;  // GlobalPara.cpp:38
     p->mesh_scale = 1.0;
     p->max_iteration = 5000;
     p->ref_area = 1.0;
@@ -334,8 +335,11 @@ extern "C" int fvgb_params_read_toml(const char* path, fvgb_params* p, char* mes
     r.integer("physicsModel.equation", p->equation, true);
     bool steady = false;
     r.boolean("time.is_steady", steady, false);
-    if (steady) return fail(FVGB_ERR_UNSUPPORTED, "time.is_steady = 1 (local time stepping) is outside this path");
-    r.num("time.CFL", p->CFL, true);
+    p->steady = steady ? 1 : 0;
+    // getValueOnCondition (TomlFileManager.h:113-130, .cpp:159-160): each is read where present
+    // and required only in its own mode
+    r.num("time.CFL_steady", p->CFL_steady, steady);
+    r.num("time.CFL", p->CFL, !steady);
     r.num("time.max_physical_time", p->T_end, true);
     r.integer("time.time_advance", p->time_advance, true);
     r.integer("inviscid_flux_method.flag_reconstruct", p->reconstruct, true);

@@ -149,6 +149,8 @@ int Solver::init(const fvgb_mesh_soa& m, const fvgb_params& prm) {
         (rc = dalloc(d_res_part, (size_t)dev::residual_blocks(N) + 1, owned)) || (rc = dalloc(d_res_out, 4, owned)))
         return rc;
     if (p.time_advance == 3103 && (rc = dalloc(d_K1, n4, owned))) return rc;
+    if (p.steady && (rc = dalloc(d_dt_local, (size_t)N, owned))) return rc;
+    cell0_dev = N > 0 ? L.cell_new[0] : 0;
     if (!d_K1) d_K1 = d_U0;  // unused by the other integrators
     CK(cudaMemsetAsync(d_flag_count, 0, sizeof(unsigned int), s));
     CK(cudaMemsetAsync(d_status, 0, sizeof(dev::Status), s));
@@ -237,7 +239,7 @@ void Solver::enqueue_stage(int kind) {
     launches += (mv.E_int > 0) + (mv.E > mv.E_int);
     mark(PROF_UPDATE, true);
     dev::launch_update(s, kind, d_U, d_U0, d_K1, d_rhs, d_F, mv, d_state, gas, d_flags, d_flag_count, kFlagCap,
-                       d_status, d_rec_R);
+                       d_status, d_rec_R, d_dt_local);
     mark(PROF_UPDATE, false);
     launches += 1;
 }
@@ -245,10 +247,23 @@ void Solver::enqueue_stage(int kind) {
 // one CIteration::iteration_device: dt, t clamp, stages, restrict
 void Solver::enqueue_step() {
     cudaStream_t s = stream;
-    const bool copy = p.time_advance != 3101;
+    const bool copy = p.time_advance != 3101 && !p.steady;
     mark(PROF_DT, true);
     dev::launch_prim(s, d_U, d_U0, d_prim, N, gas, copy);
     const double value_1 = std::max(4.0 / 3.0, p.gamma / p.Pr);
+    if (p.steady) {  // CIteration.cpp:42-52 (host) and 109-121 (device)
+        dev::launch_dt_local(s, d_prim, mv, gas, value_1, p.CFL, p.equation == 2, d_alpha, d_alpha_vis, d_dt_local,
+                             d_state, cell0_dev, d_status);
+        mark(PROF_DT, false);
+        launches += 3;
+        enqueue_stage(dev::STAGE_LOCAL);
+        mark(PROF_RESTRICT, true);  // as iteration_host does (CIteration.cpp:79); iteration_device skips it
+        dev::launch_restrict(s, d_U, mv, d_cell_ref, d_cell_new, d_flags, d_flag_count, kFlagCap, p.restrict_ref, gas,
+                             d_status);
+        mark(PROF_RESTRICT, false);
+        launches += 1;
+        return;
+    }
     dev::launch_dt(s, d_prim, mv, gas, value_1, p.CFL, p.equation == 2, d_alpha, d_alpha_vis, &d_state->dtmin_bits,
                    d_status);
     dev::launch_dt_final(s, d_state, true);

@@ -45,6 +45,8 @@ struct Solver {
     dev::EdgeTape rec_tape;  // when set (.v), the flux kernels also write the adjoint's edge tape
     dev::CellTape rec_ctape;  // when set (.gx), the gradient kernel also writes the limiter record
     double *d_alpha = nullptr, *d_alpha_vis = nullptr, *d_stage = nullptr, *d_res_out = nullptr;
+    double* d_dt_local = nullptr;  // per-cell dt of a steady run (time.is_steady = 1)
+    int cell0_dev = 0;             // device index of the reference's cell 0 (its dt moves t in steady runs)
     int* d_flags = nullptr;
     unsigned int* d_flag_count = nullptr;
     dev::StepState* d_state = nullptr;

@@ -18,10 +18,11 @@ enum StageKind {
     STAGE_SSP_1 = 5,   // SSP-RK3 (3104) stages
     STAGE_SSP_2 = 6,
     STAGE_SSP_3 = 7,
+    STAGE_LOCAL = 8,   // forward Euler with each cell's own dt (time.is_steady = 1)
 };
 
 __host__ __device__ constexpr bool final_stage(int kind) {
-    return kind == STAGE_EULER || kind == STAGE_RK3_3 || kind == STAGE_SSP_3;
+    return kind == STAGE_EULER || kind == STAGE_RK3_3 || kind == STAGE_SSP_3 || kind == STAGE_LOCAL;
 }
 
 // The stage's time offset, in units of dt, at which the double-Mach-reflection boundary is

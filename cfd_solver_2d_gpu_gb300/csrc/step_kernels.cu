@@ -88,15 +88,39 @@ __global__ void __launch_bounds__(256) k_update(d4* __restrict__ U, const d4* __
                                                 d4* __restrict__ rhs_out, const d4* __restrict__ F, MeshView m,
                                                 const StepState* s, Gas g, int* __restrict__ flag_list,
                                                 unsigned int* flag_count, int flag_cap, Status* st,
-                                                d4* __restrict__ rec_R) {
+                                                d4* __restrict__ rec_R, const double* __restrict__ dt_local) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
+    if constexpr (KIND == STAGE_LOCAL) {  // evolve_explicit_localtimestep, Evolve.cpp:115-125
+        update_cell<STAGE_EULER>(c, U, U0, K1, rhs_out, F, m, __ldg(&dt_local[c]), 0.0, g, flag_list, flag_count,
+                                 flag_cap, st, rec_R);
+        return;
+    }
     double dt = 0.0, dt6 = 0.0;
     if (KIND != STAGE_RHS) {
         dt = s->dt;
         dt6 = s->dt6;
     }
     update_cell<KIND>(c, U, U0, K1, rhs_out, F, m, dt, dt6, g, flag_list, flag_count, flag_cap, st, rec_R);
+}
+
+// get_local_dt_host/device (CalculateDt.cpp:66-72, 182-186; CalculateDtGPU.cu:83-110): each
+// cell's CFL vol / alpha; the clock moves by the dt of the reference's cell 0
+// (CIteration.cpp:47-49, 110-113) and T does not bound it
+template <bool NS>
+__global__ void __launch_bounds__(256) k_dt_local(MeshView m, const double* __restrict__ alpha,
+                                                  const double* __restrict__ alpha_vis, double CFL,
+                                                  double* __restrict__ dt_local, StepState* s, int cell0) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.N) return;
+    const double v = dt_cell<NS>(c, m, alpha, alpha_vis, CFL);
+    dt_local[c] = v;
+    if (c == cell0) {
+        s->dt_raw = v;
+        s->dt = v;
+        s->dt6 = v / 6.0;
+        s->t += v;
+    }
 }
 
 __global__ void k_restrict(d4* U, MeshView m, const int* __restrict__ cell_ref_of_dev,
@@ -190,6 +214,19 @@ void launch_dt(cudaStream_t s, const d4* prim, const MeshView& m, const Gas& g, 
 
 void launch_dt_final(cudaStream_t s, StepState* st, bool advance) { k_dt_final<<<1, 32, 0, s>>>(st, advance ? 1 : 0); }
 
+void launch_dt_local(cudaStream_t s, const d4* prim, const MeshView& m, const Gas& g, double value_1, double CFL,
+                     bool ns, double* alpha, double* alpha_vis, double* dt_local, StepState* st, int cell0,
+                     Status* status) {
+    if (m.E > 0) {
+        if (ns) k_alpha<true><<<blocks(m.E, 256), 256, 0, s>>>(prim, m, g, value_1, alpha, alpha_vis, status);
+        else k_alpha<false><<<blocks(m.E, 256), 256, 0, s>>>(prim, m, g, value_1, alpha, alpha_vis, status);
+    }
+    if (m.N > 0) {
+        if (ns) k_dt_local<true><<<blocks(m.N, 256), 256, 0, s>>>(m, alpha, alpha_vis, CFL, dt_local, st, cell0);
+        else k_dt_local<false><<<blocks(m.N, 256), 256, 0, s>>>(m, alpha, alpha_vis, CFL, dt_local, st, cell0);
+    }
+}
+
 void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const MeshView& m, d4* Gx, d4* Gy,
                  const CellTape* tape) {
     if (m.N <= 0) return;
@@ -245,12 +282,13 @@ void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, 
 
 void launch_update(cudaStream_t s, int kind, d4* U, const d4* U0, d4* K1, d4* rhs,
                    const d4* F, const MeshView& m, const StepState* st, const Gas& g, int* flag_list,
-                   unsigned int* flag_count, int flag_cap, Status* status, d4* rec_R) {
+                   unsigned int* flag_count, int flag_cap, Status* status, d4* rec_R, const double* dt_local) {
     if (m.N <= 0) return;
     const int b = blocks(m.N, 256);
 #define FVGB_UPD(K) \
-    k_update<K><<<b, 256, 0, s>>>(U, U0, K1, rhs, F, m, st, g, flag_list, flag_count, flag_cap, status, rec_R)
+    k_update<K><<<b, 256, 0, s>>>(U, U0, K1, rhs, F, m, st, g, flag_list, flag_count, flag_cap, status, rec_R, dt_local)
     switch (kind) {
+    case STAGE_LOCAL: FVGB_UPD(STAGE_LOCAL); break;
     case STAGE_RHS: FVGB_UPD(STAGE_RHS); break;
     case STAGE_EULER: FVGB_UPD(STAGE_EULER); break;
     case STAGE_RK3_1: FVGB_UPD(STAGE_RK3_1); break;

@@ -19,6 +19,9 @@ void launch_prim(cudaStream_t s, const d4* U, d4* U0, d4* prim, int N, const Gas
 void launch_dt(cudaStream_t s, const d4* prim, const MeshView& m, const Gas& g, double value_1, double CFL,
                bool ns, double* alpha, double* alpha_vis, unsigned long long* dtmin, Status* st);
 void launch_dt_final(cudaStream_t s, StepState* st, bool advance);
+void launch_dt_local(cudaStream_t s, const d4* prim, const MeshView& m, const Gas& g, double value_1, double CFL,
+                     bool ns, double* alpha, double* alpha_vis, double* dt_local, StepState* st, int cell0,
+                     Status* status);
 void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const MeshView& m, d4* Gx, d4* Gy,
                  const CellTape* tape = nullptr);
 void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, const d4* Gx,
@@ -26,7 +29,8 @@ void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, 
                  const EdgeTape* tape = nullptr);
 void launch_update(cudaStream_t s, int kind, d4* U, const d4* U0, d4* K1, d4* rhs,
                    const d4* F, const MeshView& m, const StepState* st, const Gas& g, int* flag_list,
-                   unsigned int* flag_count, int flag_cap, Status* status, d4* rec_R = nullptr);
+                   unsigned int* flag_count, int flag_cap, Status* status, d4* rec_R = nullptr,
+                   const double* dt_local = nullptr);
 void launch_restrict(cudaStream_t s, d4* U, const MeshView& m, const int* cell_ref_of_dev,
                      const int* dev_of_cell_ref, int* flag_list, unsigned int* flag_count, int flag_cap,
                      int restrict_ref, const Gas& g, Status* st);

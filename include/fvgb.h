@@ -64,6 +64,14 @@ typedef struct fvgb_params {
      * own; the reference reads CBoundaryDoubleShockReflect's t + dt there, Flux.cpp:328-332).
      * The handle-based entry points keep their own clock and ignore it. */
     double dsr_time;
+    /* time.is_steady = 1: local time stepping, each cell advanced by its own
+     * CFL vol / alpha (CIteration.cpp:42-52, CalculateDt.cpp:66-72, 182-186,
+     * Evolve.cpp:115-125); forward Euler, T is not a bound.  The step uses
+     * time.CFL (default 0.6) as the reference does; time.CFL_steady is read into
+     * CFL_steady (TomlFileManager.cpp:159-160) and not used by the step. */
+    int steady;
+    int pad2_;
+    double CFL_steady;
 } fvgb_params;
 
 /* Reference-order mesh arrays, mirroring GPU::NodeSoA / ElementSoA / EdgeSoA /

@@ -1122,6 +1122,30 @@ int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* 
     double *Us = (double*)malloc(M * sizeof(double)), *U1 = (double*)malloc(M * sizeof(double));
     int rc = 0;
     om_params ps = *p; /* ps.dsr_time: the stage's clock, CIteration.cpp:60-62 and Evolve.cpp:43-77 */
+    if (p->steady) {
+        /* iteration_host's steady branch (CIteration.cpp:42-52): get_local_dt_host
+         * (CalculateDt.cpp:66-72, 182-186), t += alphaC[0], evolve_explicit_localtimestep
+         * (Evolve.cpp:115-125), then the positivity pass (CIteration.cpp:79).  The double-
+         * Mach-reflection clock is not moved by this branch: it stays at p->dsr_time. */
+        double* aC = (double*)malloc((size_t)N * sizeof(double));
+        for (int s = 0; s < nsteps && rc == 0; s++) {
+            double dmin;
+            if ((rc = om_dt(m, p, U, &dmin, aC))) break;
+            for (int i = 0; i < N; i++) aC[i] = p->CFL * m->elem_vol[i] / aC[i];
+            *t += aC[0];
+            if (dts) dts[s] = aC[0];
+            if ((rc = om_rhs(m, p, U, k1, NULL, NULL))) break;
+            #pragma omp parallel for schedule(static)
+            for (int i = 0; i < N; i++)
+                for (int j = 0; j < 4; j++) U[(size_t)j * N + i] += aC[i] * k1[(size_t)j * N + i];
+            int r = om_restrict(m, p, U);
+            if (r < 0) rc = r == -1 ? -9 : r;
+        }
+        free(aC);
+        if (last_rhs && rc == 0) memcpy(last_rhs, k1, M * sizeof(double));
+        free(U0); free(k1); free(k2); free(k3); free(Us); free(U1);
+        return rc;
+    }
     for (int s = 0; s < nsteps; s++) {
         double dt;
         rc = om_dt(m, p, U, &dt, NULL);

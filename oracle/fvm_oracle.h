@@ -50,6 +50,8 @@ typedef struct om_params {
     double shock[4];   /* shock tube: x, y, normal x, normal y */
     double dsr[3];     /* double Mach reflection: x, y where the shock meets the wall, angle (degrees) */
     double dsr_time;   /* CBoundaryDoubleShockReflect's t + dt: the time of "dsr" edges in om_rhs */
+    int steady;        /* 1: local time stepping (time.is_steady), forward Euler with each cell's dt */
+    int pad2_;
 } om_params;
 
 /* Reads an .su2 file and assembles the mesh exactly as the reference does.
@@ -67,7 +69,8 @@ int om_dt(const om_mesh* m, const om_params* p, const double* U, double* dt, dou
 /* Positivity pass on U in place. Returns the number of cells replaced, -1 on NaN. */
 int om_restrict(const om_mesh* m, const om_params* p, double* U);
 /* nsteps steps of time_advance from time *t; U in place; dts[nsteps] may be NULL.
- * "dsr" edges are evaluated at each stage's time (p->dsr_time is not used). */
+ * "dsr" edges are evaluated at each stage's time (p->dsr_time is not used).
+ * Steady runs advance each cell by its own dt and t by cell 0's (dts: those). */
 int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* t, double* dts, double* last_rhs);
 /* Residual norm of an RHS field: norm 0 = L-infinity, 1 = L1, 2 = L2 (per variable). */
 void om_residual(const om_mesh* m, const double* rhs, int norm, double* out4);

@@ -35,7 +35,8 @@ class OmParams(ctypes.Structure):
                                            "time_advance", "lsq_det_ref", "wall_bc_ref", "restrict_ref", "pad_")] + [
         (n, ctypes.c_double) for n in ("gamma", "R", "Pr", "mu0", "T0", "CFL", "T_end")] + [
         ("inf", ctypes.c_double * 4), ("inlet", ctypes.c_double * 4), ("outlet", ctypes.c_double * 4),
-        ("shock", ctypes.c_double * 4), ("dsr", ctypes.c_double * 3), ("dsr_time", ctypes.c_double)]
+        ("shock", ctypes.c_double * 4), ("dsr", ctypes.c_double * 3), ("dsr_time", ctypes.c_double),
+        ("steady", ctypes.c_int), ("pad2_", ctypes.c_int)]
 
 
 def build():
@@ -181,7 +182,8 @@ def params_from_toml(cfg):
     else:
         p.mu0 = float(g("constant.mu0", 17.9e-6))
     p.equation = int(g("physicsModel.equation", 1))
-    p.CFL = float(g("time.CFL", 0.6))
+    p.CFL = float(g("time.CFL", 0.6))  # also in steady runs: time.CFL_steady is not used (TomlFileManager.cpp:159-160)
+    p.steady = 1 if int(g("time.is_steady", 0)) else 0
     p.T_end = float(g("time.max_physical_time", 20))
     p.time_advance = int(g("time.time_advance", 3101))
     p.reconstruct = int(g("inviscid_flux_method.flag_reconstruct", 3001))

@@ -104,6 +104,15 @@ def golden_cases(d):
         ("sod_tilted_channel24_llf_lsq_barth_ssp", T(flux=2001, reconstruct=3002, gradient=1, limiter=1,
                                                      time_advance=3104, CFL=0.5, shock_tube=(5.0, 5.0, 0.6, 0.8),
                                                      **sod), ch24j, "ssprk3", 10),
+        # steady runs (local time stepping through iteration_host): the cylinder with time.CFL given,
+        # the channel without it (the reference's default CFL 0.6; time.CFL_steady is not used)
+        ("cylinder32_euler_roe_lsq_steady", T(equation=1, flux=2002, reconstruct=3002, gradient=1, limiter=1,
+                                              time_advance=3101, CFL=0.8, steady=True, ic_type=1, inf_mode=0,
+                                              Ma=0.5), cyl, "euler", 30),
+        ("jchannel24_llf_o1_steady", T(flux=2001, reconstruct=3001, gradient=1, limiter=1, time_advance=3101,
+                                       CFL=None, steady=True, CFL_steady=0.3, vortex=(2.5, 7.0, 5.0),
+                                       inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0),
+                                       outlet=(1.0, 1.0, 0.0, 0.9)), ch24j, "euler", 30),
     ]
 
 

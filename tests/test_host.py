@@ -53,7 +53,7 @@ def test_toml_matches_reference_semantics(name):
     tp, _, _ = make_golden.load(name)
     p = fv.Params.from_toml(tp)
     q, info = params_from_toml(tp)
-    for k in ("equation", "flux_scheme", "reconstruct", "gradient", "limiter", "time_advance"):
+    for k in ("equation", "flux_scheme", "reconstruct", "gradient", "limiter", "time_advance", "steady"):
         assert getattr(p, k) == getattr(q, k), k
     for k in ("gamma", "R", "Pr", "mu0", "T0", "CFL", "T_end"):
         assert getattr(p, k) == pytest.approx(getattr(q, k), rel=1e-15), k
@@ -176,3 +176,30 @@ def test_double_mach_reflection_and_shock_tube_inputs(tmp_path):
     assert list(p.shock) == [0.0, 0.0, 1.0, 0.0]
     U = fv.initial_field(fv.Mesh.read_su2(sp, p), p)
     assert np.all(U[0] == 0.125)  # every centroid lies at x > 0: downstream of the default shock
+
+
+def test_steady_inputs(tmp_path):
+    """time.is_steady = 1 (TomlFileManager.cpp:158-160): time.CFL_steady is required and
+    time.CFL optional (default 0.6), and the step uses time.CFL, as the reference does;
+    the batched form and the adjoint step in time only."""
+    tp = tmp_path / "s.toml"
+    tp.write_text(cases.toml_text(steady=True, CFL=None, CFL_steady=0.3))
+    p = fv.Params.from_toml(str(tp))
+    assert (p.steady, p.CFL, p.CFL_steady) == (1, 0.6, 0.3)
+    q, _ = params_from_toml(str(tp))
+    assert (q.steady, q.CFL) == (1, 0.6)
+    tp.write_text(cases.toml_text(steady=True, CFL=0.45).replace("CFL_steady = 0.8\n", ""))
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Params.from_toml(str(tp))
+    assert "time.CFL_steady" in str(e.value)
+    tp.write_text(cases.toml_text(CFL=None))
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Params.from_toml(str(tp))
+    assert "time.CFL" in str(e.value)
+    tp.write_text(cases.toml_text(steady=True, CFL=0.45))
+    p = fv.Params.from_toml(str(tp))
+    assert (p.steady, p.CFL) == (1, 0.45)
+    m = fv.Mesh.read_su2(cases.square_mesh(8, directory=str(tmp_path)), p)
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Batch([m], [p])
+    assert "is_steady" in str(e.value)
