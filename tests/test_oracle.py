@@ -100,34 +100,43 @@ def test_live_reference_larger_mesh(tmp_path):
     assert np.array_equal(U, ref["U"])
 
 
-REF_DSR = os.path.join(os.path.dirname(REF), "quick_start", "U2NITS-10.0", "2D_double_shock_reflect")
+REF_CASES = os.path.join(os.path.dirname(REF), "quick_start", "U2NITS-10.0")
+# the reference's example cases (folder, mesh) and what each exercises
+EXAMPLES = [
+    ("2D_isentropic_vortex", "ivortex50.su2"),        # periodic vortex, Green-Gauss, Roe
+    ("2D_cylinder", "cylinder_allfar_50.su2"),       # laminar cylinder, no-slip wall, far field
+    ("1D_shocktube", "shocktube_100.su2"),           # shock tube along x
+    ("2D_Neuvillette_shock", "neuvillette.su2"),     # shock tube with the normal along y, laminar
+    ("2D_double_shock_reflect", "dsr131new_slippery.su2"),  # "dsr" boundary, input_mode 3, laminar
+]
 
 
-@pytest.mark.skipif(not (os.path.exists(REF) and os.path.isdir(REF_DSR)),
+@pytest.mark.skipif(not (os.path.exists(REF) and os.path.isdir(REF_CASES)),
                     reason="the reference (sources and oracle/_ref build) is only in the build container")
-def test_live_reference_own_double_mach_reflection_case(tmp_path):
-    """The reference's own double-Mach-reflection example (dsr131new_slippery.su2 with its
-    input.toml: "dsr" top boundary, input_mode 3 inlet, Navier-Stokes, Green-Gauss), its
-    mesh, initial field and 5 forward-Euler steps run by the reference binary and by the
-    oracle: identical bits."""
+@pytest.mark.parametrize("folder,mesh", EXAMPLES)
+def test_live_reference_own_examples(tmp_path, folder, mesh):
+    """The reference's own example cases as shipped (mesh and input.toml), their mesh
+    arrays, initial field and 5 forward-Euler steps run by the reference binary and by the
+    oracle: identical bits; and this library's reader, input.toml and initial field on
+    the same files."""
     from fvmrdump import read_dump
-    su2 = os.path.join(REF_DSR, "dsr131new_slippery.su2")
-    tp = os.path.join(REF_DSR, "input.toml")
+    su2 = os.path.join(REF_CASES, folder, mesh)
+    tp = os.path.join(REF_CASES, folder, "input.toml")
     out = tmp_path / "r.bin"
     subprocess.run([REF, tp, su2, "euler", "5", str(out)], check=True, capture_output=True)
     ref = read_dump(str(out))
     o = Oracle(tp, su2)
     for k, v in MESH.items():
         assert np.array_equal(o.array(v), np.asarray(ref[k]).reshape(o.array(v).shape)), k
-    assert 6014 in ref["bc_type"]
     U0 = o.init_field()
     assert np.array_equal(U0, ref["U0"].reshape(U0.shape))
     o.params.time_advance = 3101
     U, t, _, _ = o.run(U0, 5)
     assert np.array_equal(U, ref["U"].reshape(U.shape)) and t == ref["t"][0]
-    # this library's reader, input.toml and initial field on the same case
     import cfd_solver_2d_gpu_gb300 as fv
     p = fv.Params.from_toml(tp)
     m = fv.Mesh.read_su2(su2, p)
-    assert np.array_equal(m.array("edge_xy"), o.array("edge_xy")) and list(p.dsr) == [0.6, 0.0, 60.0]
+    for ours, theirs in (("edge_xy", "edge_xy"), ("edge_normal", "edge_normal"), ("elem_neighbors", "elem_nbrs"),
+                         ("boundary_type", "bc_type")):
+        assert np.array_equal(m.array(ours).ravel(), o.array(theirs).ravel()), ours
     assert np.array_equal(fv.initial_field(m, p), U0)
