@@ -1,8 +1,9 @@
 // Discrete adjoint of the explicit step (no counterpart in the reference).
 //
-// For U_{n+1} = Step(U_n) (time step, Runge-Kutta stages; forward Euler 3101 or
-// SSP-RK3 3104; Euler equations; least-squares gradients with or without the
-// Barth limiter; Roe flux; interior, periodic and slip-wall edges) this
+// For U_{n+1} = Step(U_n) (time step, Runge-Kutta stages; forward Euler 3101,
+// Kutta RK3 3103 or SSP-RK3 3104; Euler equations; least-squares gradients with or
+// without the Barth limiter; Roe flux; interior, periodic, slip-wall, symmetry,
+// far-field, inlet and outlet edges) this
 // computes lambda_0 = (dU_K/dU_0)^T lambda_K by reverse sweeps over the steps,
 // each stage's vector-Jacobian product being the hand-written reverse of the
 // forward kernels (adjoint_device.cuh).  The time step's dependence on the
@@ -48,7 +49,7 @@ constexpr int kEdgeThreads = 128;
 // mu = dLoss/dF_e (F_e enters R_L with +1/-vol and, when e is in R's edge list, R_R with
 // -1/-vol), then the flux VJP from the stage's recorded tape: the face states and the
 // Roe intermediates are read, not recomputed
-__global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView m, Gas g,
+__global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView m, Gas g, BcData bc,
                                                            const d4* __restrict__ lam,
                                                            const int* __restrict__ e_rlist, d4* __restrict__ aL,
                                                            d4* __restrict__ aR) {
@@ -82,8 +83,12 @@ __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView
     d4 bfL, bfR;
     roe_rev(wL, wR, fL, fR, nx, ny, len, g, r, mu, bwL, bwR, bfL, bfR);
     to_prim_vjp(fR, wR, g, bwR, bfR);
-    if (e >= m.E_int) {  // slip wall / symmetry: the ghost is a function of the L face state
-        ghost_slip_vjp(fL, wL, nx, ny, bfR, bfL, bwL);
+    if (e >= m.E_int) {  // a boundary edge: the ghost is a function of the L face state
+        const int bt = __ldg(&m.e_bc[e]);
+        if (bt == 6011) ghost_farfield_vjp(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, bfR, bwL);
+        else if (bt == 6012) ghost_farfield_vjp(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, bfR, bwL);
+        else if (bt == 6013) ghost_farfield_vjp(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, bfR, bwL);
+        else ghost_slip_vjp(fL, wL, nx, ny, bfR, bfL, bwL);  // slip wall, symmetry
         bfR = mk4(0, 0, 0, 0);
     }
     to_prim_vjp(fL, wL, g, bwL, bfL);
@@ -181,14 +186,16 @@ __global__ void __launch_bounds__(256) k_adj_cell(MeshView m, const d4* __restri
 }
 
 // ---- per cell: neighbours' LSQ adjoints and the stage's Runge-Kutta combination ------
-// U_s = a U_0 + b (U_in + dt R(U_in)):  lam_in = b (lam_s + dt J^T lam_s);  acc0 (+)= a lam_s.
+// U_s = a U_0 + b (c U_in + dt R(U_in)):  lam_in = b (c lam_s + dt J^T lam_s);  acc0 (+)= a lam_s.
+// (c = 1 for forward Euler and SSP-RK3; the Kutta stages pass their residual's seed as lam_s
+// with c = 0 and combine the results with k_adj_lincomb.)
 // acc_mode 0: acc0 = a lam_s; 1: acc0 += a lam_s; 2: nothing; 3 (a = 0, the first stage, whose
 // input is U_0 itself): lam_in += acc0.  dot_part[block] = sum over the block's cells of
 // lam_s . R_s (= d loss / d dt through this stage, divided by b), summed in a fixed order.
 __global__ void __launch_bounds__(256) k_adj_combine(MeshView m, const int* __restrict__ rev,
                                                      const d4* __restrict__ lam_dir, const d4* __restrict__ bdU,
                                                      const d4* __restrict__ lam_s, const d4* __restrict__ R_s,
-                                                     const double* __restrict__ dt_p, double a, double b,
+                                                     const double* __restrict__ dt_p, double a, double b, double ci,
                                                      int acc_mode, d4* __restrict__ lam_in, d4* __restrict__ acc0,
                                                      int linear, double* __restrict__ dot_part) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -210,7 +217,8 @@ __global__ void __launch_bounds__(256) k_adj_combine(MeshView m, const int* __re
         const d4 ls = ld4(&lam_s[c]);
         const d4 rs = ld4(&R_s[c]);
         dot = fma(ls.x, rs.x, fma(ls.y, rs.y, fma(ls.z, rs.z, ls.w * rs.w)));
-        d4 li = mk4(b * fma(dt, r[0], ls.x), b * fma(dt, r[1], ls.y), b * fma(dt, r[2], ls.z), b * fma(dt, r[3], ls.w));
+        d4 li = mk4(b * fma(dt, r[0], ci * ls.x), b * fma(dt, r[1], ci * ls.y), b * fma(dt, r[2], ci * ls.z),
+                    b * fma(dt, r[3], ci * ls.w));
         if (acc_mode == 0) {
             acc0[c] = mk4(a * ls.x, a * ls.y, a * ls.z, a * ls.w);
         } else if (acc_mode == 1) {
@@ -231,6 +239,27 @@ __global__ void __launch_bounds__(256) k_adj_combine(MeshView m, const int* __re
         for (int i = 0; i < 8; i++) t += sm[i];
         dot_part[blockIdx.x] = t;
     }
+}
+
+// out = c0 x0 + c1 x1 + c2 x2 + c3 x3 per cell (null terms skipped): the Kutta stages' seeds
+__global__ void __launch_bounds__(256) k_adj_lincomb(int n, d4* out, double c0, const d4* x0,
+                                                     double c1, const d4* x1, double c2, const d4* x2, double c3,
+                                                     const d4* x3) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const double cs[4] = {c0, c1, c2, c3};
+    const d4* xs[4] = {x0, x1, x2, x3};
+    double r[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (!xs[k]) continue;
+        const d4 x = ld4(&xs[k][c]);
+        r[0] = fma(cs[k], x.x, r[0]);
+        r[1] = fma(cs[k], x.y, r[1]);
+        r[2] = fma(cs[k], x.z, r[2]);
+        r[3] = fma(cs[k], x.w, r[3]);
+    }
+    out[c] = mk4(r[0], r[1], r[2], r[3]);
 }
 
 // smallest cell index whose CFL vol / alpha equals the step's minimum
@@ -358,6 +387,7 @@ struct Adjoint {
     double* d_seg_dt = nullptr;    // per step: dt, dt_raw
     int* d_seg_cstar = nullptr;    // per step: the minimising cell
     d4 *d_lam = nullptr, *d_lam_in = nullptr, *d_acc0 = nullptr, *d_aL = nullptr, *d_aR = nullptr;
+    d4 *d_k_a2 = nullptr, *d_k_a1 = nullptr, *d_k_seed = nullptr;  // Kutta RK3: lam_U2, lam_U1, a seed
     d4 *d_lamdir = nullptr, *d_bdU = nullptr, *d_keepU = nullptr;
     int *d_rlist = nullptr, *d_rev = nullptr;
     double* d_dotp = nullptr;
@@ -383,14 +413,16 @@ struct Adjoint {
         if (p.equation != 1) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers the Euler equations");
         if (p.steady) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers time-accurate runs (time.is_steady = 0)");
         if (p.flux_scheme != 2002) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers the Roe flux");
-        if (p.time_advance != 3101 && p.time_advance != 3104)
-            return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers forward Euler (3101) and SSP-RK3 (3104)");
+        if (p.time_advance != 3101 && p.time_advance != 3103 && p.time_advance != 3104)
+            return fail(FVGB_ERR_ARG, "invalid time_advance");
         if (p.reconstruct == 3002 && p.gradient != 1)
             return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers least-squares gradients");
         for (int e = s->L.E_int; e < s->E; e++) {
             const int bt = s->L.e_bc[e];
-            if (bt != 6001 && bt != 6021)
-                return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers interior, periodic and slip-wall edges");
+            if (bt != 6001 && bt != 6021 && bt != 6011 && bt != 6012 && bt != 6013)
+                return fail(FVGB_ERR_UNSUPPORTED,
+                            "the adjoint covers interior, periodic, slip-wall, symmetry, far-field, inlet and "
+                            "outlet edges");
         }
         K = nsteps;
         ncheck = std::max(1, std::min(ncheck, K));
@@ -442,6 +474,9 @@ struct Adjoint {
             (rc = alloc(d_lamdir, N)) || (rc = alloc(d_keepU, N)) || (rc = alloc(d_bdU, 3 * (size_t)N)) ||
             (rc = alloc(d_dotp, (size_t)nb * 3)))
             return rc;
+        if (p.time_advance == 3103 &&
+            ((rc = alloc(d_k_a2, N)) || (rc = alloc(d_k_a1, N)) || (rc = alloc(d_k_seed, N))))
+            return rc;
         return 0;
     }
 
@@ -473,11 +508,12 @@ struct Adjoint {
         if (v.p.time_advance == 3101) {
             stage(0, dev::STAGE_EULER);
         } else {
-            stage(0, dev::STAGE_SSP_1);
+            const bool kutta = v.p.time_advance == 3103;
+            stage(0, kutta ? dev::STAGE_RK3_1 : dev::STAGE_SSP_1);
             AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst + 1], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
-            stage(1, dev::STAGE_SSP_2);
+            stage(1, kutta ? dev::STAGE_RK3_2 : dev::STAGE_SSP_2);
             AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst + 2], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
-            stage(2, dev::STAGE_SSP_3);
+            stage(2, kutta ? dev::STAGE_RK3_3 : dev::STAGE_SSP_3);
         }
         v.d_rec_R = nullptr;
         v.rec_tape = dev::EdgeTape();
@@ -488,23 +524,26 @@ struct Adjoint {
         return 0;
     }
 
-    // one stage VJP: lam_s (d_lam) -> lam_in (d_lam_in), acc0, partial F.mu in dot slot;
-    // (Uin, Gx, Gy): the stage's input state and the limited gradients the forward used
+    // one stage VJP: lam_s (seed, default d_lam) -> lam_in (out, default d_lam_in), acc0,
+    // partial lam_s . R_s in dot slot; tape and ct: the stage's records of its input state
     int stage_vjp(const d4* Uin, const dev::EdgeTape& tape, const dev::CellTape& ct, const d4* Rs,
-                  const double* dt_p, double a, double b, int acc_mode, int dot_slot) {
+                  const double* dt_p, double a, double b, int acc_mode, int dot_slot, const d4* seed = nullptr,
+                  d4* out = nullptr, double ci = 1.0) {
+        if (!seed) seed = d_lam;
+        if (!out) out = d_lam_in;
         Solver& v = *s;
         cudaStream_t st = v.stream;
         const bool linear = v.p.reconstruct == 3002;
         const int nbE = nblk(v.E, dev::kEdgeThreads), nbN = nblk(v.N, 256);
         double* dp = d_dotp + (size_t)dot_slot * nbN;
-        dev::k_adj_edge<<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, d_lam, d_rlist, d_aL, d_aR);
+        dev::k_adj_edge<<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, v.bc, seed, d_rlist, d_aL, d_aR);
         const int* fl = tape.flags;
         if (!linear) dev::k_adj_cell<false, false><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU);
         else if (v.p.limiter == 1)
             dev::k_adj_cell<true, true><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU);
         else dev::k_adj_cell<true, false><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU);
-        dev::k_adj_combine<<<nbN, 256, 0, st>>>(v.mv, d_rev, d_lamdir, d_bdU, d_lam, Rs, dt_p, a, b, acc_mode,
-                                                d_lam_in, d_acc0, linear ? 1 : 0, dp);
+        dev::k_adj_combine<<<nbN, 256, 0, st>>>(v.mv, d_rev, d_lamdir, d_bdU, seed, Rs, dt_p, a, b, ci, acc_mode,
+                                                out, d_acc0, linear ? 1 : 0, dp);
         AK(cudaGetLastError());
         return 0;
     }
@@ -532,6 +571,32 @@ struct Adjoint {
             // U1 = U0 + dt R(U0): a = 0, b = 1
             if ((rc = stage_vjp(seg_states[(size_t)slot], tp(0), ctp(0), R(0), dtp, 0.0, 1.0, 2, 0))) return rc;
             std::swap(d_lam, d_lam_in);
+        } else if (v.p.time_advance == 3103) {
+            // Kutta RK3: k1 = R(U0), U1 = U0 + dt/2 k1; k2 = R(U1), U2 = U0 - dt k1 + 2 dt k2;
+            // k3 = R(U2), U3 = U0 + dt/6 (k1 + 4 k2 + k3).  With L3 = lam (adjoint of U3), the
+            // residuals' seeds (adjoints of the k, divided by dt) are
+            //   s3 = L3/6,  s2 = 2/3 L3 + 2 L2,  s1 = L3/6 - L2 + L1/2,
+            // L2 = dt J2^T s3 and L1 = dt J1^T s2 being the adjoints of U2 and U1, and
+            //   lam_U0 = L3 + L2 + L1 + dt J0^T s1;  d loss / d dt = s3.k3 + s2.k2 + s1.k1.
+            const d4* U0 = seg_states[(size_t)slot * 3];
+            const d4* U1 = seg_states[(size_t)slot * 3 + 1];
+            const d4* U2 = seg_states[(size_t)slot * 3 + 2];
+            const int nbk = nblk(v.N, 256);
+            // L2 = dt J2^T (L3/6): seed L3, b = 1/6, no identity term
+            if ((rc = stage_vjp(U2, tp(2), ctp(2), R(2), dtp, 0.0, 1.0 / 6.0, 2, 0, d_lam, d_k_a2, 0.0))) return rc;
+            dev::k_adj_lincomb<<<nbk, 256, 0, st>>>(v.N, d_k_seed, 2.0 / 3.0, d_lam, 2.0, d_k_a2, 0.0, nullptr, 0.0,
+                                                    nullptr);
+            // L1 = dt J1^T s2
+            if ((rc = stage_vjp(U1, tp(1), ctp(1), R(1), dtp, 0.0, 1.0, 2, 1, d_k_seed, d_k_a1, 0.0))) return rc;
+            dev::k_adj_lincomb<<<nbk, 256, 0, st>>>(v.N, d_k_seed, 1.0 / 6.0, d_lam, -1.0, d_k_a2, 0.5, d_k_a1, 0.0,
+                                                    nullptr);
+            // dt J0^T s1, then lam_U0
+            if ((rc = stage_vjp(U0, tp(0), ctp(0), R(0), dtp, 0.0, 1.0, 2, 2, d_k_seed, d_lam_in, 0.0))) return rc;
+            dev::k_adj_lincomb<<<nbk, 256, 0, st>>>(v.N, d_lam, 1.0, d_lam, 1.0, d_k_a2, 1.0, d_k_a1, 1.0, d_lam_in);
+            AK(cudaGetLastError());
+            b0 = 1.0 / 6.0;  // slot 0 holds L3 . k3
+            b1 = 1.0;
+            b2 = 1.0;
         } else {
             const d4* U0 = seg_states[(size_t)slot * 3];
             const d4* U1 = seg_states[(size_t)slot * 3 + 1];

@@ -192,5 +192,75 @@ __device__ __forceinline__ void ghost_slip_vjp(const d4 UL, const Prim& wL, doub
     bwL.v += b_unL * ny - b_utL * nx;
 }
 
+// adjoint of ghost_farfield (physics.cuh; get_UR_farField, FVMR/src/space/Flux.cpp:81-163):
+// bUR, the adjoint of the ghost's conserved state, onto the interior face state's primitive
+// variables (bw; .ir carries the 1/rho the sound speed reads).  The branch is re-evaluated
+// with the forward's operations on the same inputs, so it is the forward's branch.
+__device__ __forceinline__ void ghost_farfield_vjp(const Prim& e, const double* fs, double fa, double fson,
+                                                   double nx, double ny, const Gas& g, const d4 bUR, Prim& bw) {
+    const double ae = sqrt(g.gamma * e.p * e.ir);
+    const double qnf = fs[1] * nx + fs[2] * ny;
+    const double qne = e.u * nx + e.v * ny;
+    const double rf = qnf - 2.0 * fa * g.inv_ga1;
+    const double re = qne + 2.0 * ae * g.inv_ga1;
+    const double qn = 0.5 * (re + rf);
+    const double as = g.ga1 * (re - rf) * 0.25;
+    if (qn <= -as) return;  // supersonic inflow: the ghost is the far-field state
+    double r0, u0, v0, son = 0.0, X = 0.0;
+    const bool outflow = !(qn < 0);
+    if (qn < as) {
+        double qtx, qty;
+        if (!outflow) {
+            son = fson;
+            qtx = fs[1] - qnf * nx;
+            qty = fs[2] - qnf * ny;
+        } else {
+            son = e.p / pow(e.r, g.gamma);
+            qtx = e.u - qne * nx;
+            qty = e.v - qne * ny;
+        }
+        X = as * as / son * g.inv_gamma;
+        r0 = pow(X, g.inv_ga1);
+        u0 = qtx + qn * nx;
+        v0 = qty + qn * ny;
+    } else {
+        r0 = e.r; u0 = e.u; v0 = e.v;
+    }
+    // to_cons: (r, r u, r v, p/(gamma-1) + r (u^2 + v^2)/2)
+    const double br0 = bUR.x + bUR.y * u0 + bUR.z * v0 + 0.5 * bUR.w * (u0 * u0 + v0 * v0);
+    const double bu0 = (bUR.y + bUR.w * u0) * r0;
+    const double bv0 = (bUR.z + bUR.w * v0) * r0;
+    const double bp0 = bUR.w * g.inv_ga1;
+    if (!(qn < as)) {  // supersonic outflow: the ghost is the interior state
+        bw.r += br0; bw.u += bu0; bw.v += bv0; bw.p += bp0;
+        return;
+    }
+    // p0 = as^2 r0 / gamma, r0 = X^(1/(gamma-1)), X = as^2 / (son gamma)
+    double b_as = bp0 * 2.0 * as * r0 * g.inv_gamma;
+    const double b_r0 = br0 + bp0 * as * as * g.inv_gamma;
+    const double b_X = b_r0 * g.inv_ga1 * r0 / X;
+    b_as += b_X * 2.0 * as / son * g.inv_gamma;
+    const double b_son = -b_X * X / son;
+    // u0 = qtx + qn nx, v0 = qty + qn ny
+    const double b_qn = bu0 * nx + bv0 * ny;
+    double b_qne = 0.0;
+    if (outflow) {  // qtx = u - qne nx, qty = v - qne ny, son = p / r^gamma
+        bw.u += bu0;
+        bw.v += bv0;
+        b_qne -= bu0 * nx + bv0 * ny;
+        bw.p += b_son * son / e.p;
+        bw.r -= b_son * g.gamma * son / e.r;
+    }
+    // qn = (re + rf)/2, as = (gamma-1)(re - rf)/4, re = qne + 2 ae/(gamma-1)
+    const double b_re = 0.5 * b_qn + 0.25 * g.ga1 * b_as;
+    b_qne += b_re;
+    const double b_ae = 2.0 * g.inv_ga1 * b_re;
+    bw.u += b_qne * nx;
+    bw.v += b_qne * ny;
+    // ae = sqrt(gamma p ir)
+    bw.p += b_ae * g.gamma * e.ir / (2.0 * ae);
+    bw.ir += b_ae * g.gamma * e.p / (2.0 * ae);
+}
+
 }  // namespace dev
 }  // namespace fvgb

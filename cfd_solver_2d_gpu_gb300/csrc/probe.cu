@@ -9,6 +9,7 @@
 #include <string>
 
 #include "internal.h"
+#include "physics.cuh"
 
 namespace {
 
@@ -27,6 +28,12 @@ __global__ void __launch_bounds__(kThreads) k_fma_chain(double* __restrict__ out
 #pragma unroll
     for (int j = 0; j < kChains; j++) s += x[j];
     out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// the library's reciprocal on n values
+__global__ void k_math_eval(const double* __restrict__ x, double* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = fvgb::dev::rcp(x[i]);
 }
 
 }  // namespace
@@ -71,5 +78,22 @@ extern "C" int fvgb_fp64_peak(int device, double* gflops) {
     cudaEventDestroy(e1);
     const double flop = 2.0 * kChains * (double)iters * grid * kThreads;  // an FMA is two flops
     *gflops = flop / (best * 1e-3) / 1e9;
+    return 0;
+}
+
+// No counterpart in the reference: the device reciprocal rcp (physics.cuh) evaluated on
+// n host values, for accuracy tests against correctly rounded results.
+extern "C" int fvgb_math_eval(int device, int n, const double* x, double* out) {
+    if (n < 0 || (n > 0 && (!x || !out))) return fvgb::fail(FVGB_ERR_ARG, "fvgb_math_eval: bad arguments");
+    if (n == 0) return 0;
+    double* buf = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    PK(cudaSetDevice(device));
+    PK(cudaMalloc(&buf, sizeof(double) * 2 * (size_t)n));
+    PK(cudaMemcpy(buf, x, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice));
+    k_math_eval<<<(n + 255) / 256, 256>>>(buf, buf + n, n);
+    PK(cudaGetLastError());
+    PK(cudaMemcpy(out, buf + n, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost));
+    cudaFree(buf);
     return 0;
 }

@@ -384,7 +384,8 @@ __device__ __forceinline__ bool dsr_upstream(double x, double y, const BcData& b
 
 // a boundary edge with a ghost state (walls, far field, inlet, outlet, symmetry,
 // double Mach reflection); with REC
-// (Roe, Euler) the tape entry of slip-wall and symmetry edges is written as well
+// (Roe, Euler) the tape entry of slip-wall, symmetry, far-field, inlet and outlet edges is
+// written as well
 template <int FLUX, bool LINEAR, bool NS, bool REC = false>
 __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, const d4* __restrict__ Gx,
                                               const d4* __restrict__ Gy, const MeshView& m, const Gas& g,
@@ -402,11 +403,19 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
     }
     Prim wL;
     if constexpr (REC) {
-        if (bt == 6001 || bt == 6021) {
+        if (bt == 6001 || bt == 6021 || bt == 6011 || bt == 6012 || bt == 6013) {
         static_assert(!REC || (FLUX == FLUX_ROE && !NS), "the adjoint's tape covers the Roe flux of the Euler equations");
         bool usedL = false;
         const d4 fL = face_state_used<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL, usedL);
-        const d4 fR = ghost_slip(fL, wL, nx, ny);
+        d4 fR;
+        if (bt == 6001 || bt == 6021) {
+            fR = ghost_slip(fL, wL, nx, ny);
+        } else {
+            const bool ok = bt == 6011   ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
+                            : bt == 6012 ? ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR)
+                                         : ghost_farfield(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, fR);
+            if (!ok) atomicAdd(&st->farfield_oor, 1ull);
+        }
         const Prim wR = to_prim(fR, g);
         RoeRec r;
         F[e] = roe_core<true>(wL, wR, fL, fR, nx, ny, len, g, &r);

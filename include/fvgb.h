@@ -256,9 +256,9 @@ int fvgb_output_timed(fvgb_handle* h, int reps, double* ms_node_field, double* m
 /* ---- discrete adjoint ------------------------------------------------------
  * No counterpart in the reference.  Reverse-mode derivative of K steps of the
  * handle's own step map U_0 -> U_K (Euler equations, Roe flux, least-squares
- * gradients with or without the Barth limiter, forward Euler or SSP-RK3,
- * interior / periodic / slip-wall edges; the time step's dependence on the
- * state included).  fvgb_adjoint_forward runs the K steps from U0 at time t0
+ * gradients with or without the Barth limiter, forward Euler, Kutta RK3 or
+ * SSP-RK3, interior / periodic / slip-wall / symmetry / far-field / inlet /
+ * outlet edges; the time step's dependence on the state included).  fvgb_adjoint_forward runs the K steps from U0 at time t0
  * keeping n_checkpoints states (sqrt(K) keeps memory at O(sqrt(K) N)) and
  * returns U_K; fvgb_adjoint_backward then maps a seed dL/dU_K to dL/dU_0
  * (both [4][N], reference numbering), recomputing each segment once.  The
@@ -328,6 +328,12 @@ int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params* p, const 
  * on every SM (best of three timed launches): the roofline denominator for
  * kernels bound by the FP64 pipe. */
 int fvgb_fp64_peak(int device, double* gflops);
+
+/* No counterpart in the reference.  The device reciprocal the kernels use in
+ * place of most divisions (the hardware approximation refined by a series
+ * step) evaluated on n host values x on the given device: out[i] = 1/x[i].
+ * For accuracy tests. */
+int fvgb_math_eval(int device, int n, const double* x, double* out);
 
 const char* fvgb_last_error(void);
 const char* fvgb_version(void);
