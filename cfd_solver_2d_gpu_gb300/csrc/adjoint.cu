@@ -1,8 +1,8 @@
 // Discrete adjoint of the explicit step (no counterpart in the reference).
 //
 // For U_{n+1} = Step(U_n) (time step, Runge-Kutta stages; forward Euler 3101,
-// Kutta RK3 3103 or SSP-RK3 3104; Euler equations; least-squares gradients with or
-// without the Barth limiter; Roe flux; interior, periodic, slip-wall, symmetry,
+// Kutta RK3 3103 or SSP-RK3 3104; Euler equations; least-squares or Green-Gauss gradients
+// with or without the Barth limiter; Roe or LLF flux; interior, periodic, slip-wall, symmetry,
 // far-field, inlet and outlet edges) this
 // computes lambda_0 = (dU_K/dU_0)^T lambda_K by reverse sweeps over the steps,
 // each stage's vector-Jacobian product being the hand-written reverse of the
@@ -49,6 +49,7 @@ constexpr int kEdgeThreads = 128;
 // mu = dLoss/dF_e (F_e enters R_L with +1/-vol and, when e is in R's edge list, R_R with
 // -1/-vol), then the flux VJP from the stage's recorded tape: the face states and the
 // Roe intermediates are read, not recomputed
+template <int FLUX>
 __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView m, Gas g, BcData bc,
                                                            const d4* __restrict__ lam,
                                                            const int* __restrict__ e_rlist, d4* __restrict__ aL,
@@ -73,15 +74,19 @@ __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView
     Prim wR{t(T_RR), t(T_RU), t(T_RV), t(T_RP), t(T_RIR)};
     const d4 fL = mk4(wL.r, t(T_ULY), t(T_ULZ), t(T_ULW));
     const d4 fR = mk4(wR.r, t(T_URY), t(T_URZ), t(T_URW));
-    RoeRec r;
-    r.ruL = t(T_RUL); r.ruR = t(T_RUR); r.HL = t(T_HL); r.HR = t(T_HR); r.irm = t(T_IRM); r.rm = t(T_RM);
-    r.rrorl = t(T_RRORL); r.w = t(T_W); r.um = t(T_UM); r.vm = t(T_VM); r.Hm = t(T_HM); r.am2 = t(T_AM2);
-    r.iam = t(T_IAM); r.am = t(T_AM); r.un = t(T_UN); r.sel = t(T_SEL); r.Mstar = t(T_MSTAR); r.dE = t(T_DE);
-    r.Etm = t(T_ETM); r.ae = t(T_AE); r.dUroe = t(T_DUROE); r.dProe = t(T_DPROE); r.dUr = t(T_DUR);
-    r.sub = (__ldg(&tp.flags[e]) & 4) != 0;
     Prim bwL, bwR;
     d4 bfL, bfR;
-    roe_rev(wL, wR, fL, fR, nx, ny, len, g, r, mu, bwL, bwR, bfL, bfR);
+    if constexpr (FLUX == FLUX_ROE) {
+        RoeRec r;
+        r.ruL = t(T_RUL); r.ruR = t(T_RUR); r.HL = t(T_HL); r.HR = t(T_HR); r.irm = t(T_IRM); r.rm = t(T_RM);
+        r.rrorl = t(T_RRORL); r.w = t(T_W); r.um = t(T_UM); r.vm = t(T_VM); r.Hm = t(T_HM); r.am2 = t(T_AM2);
+        r.iam = t(T_IAM); r.am = t(T_AM); r.un = t(T_UN); r.sel = t(T_SEL); r.Mstar = t(T_MSTAR); r.dE = t(T_DE);
+        r.Etm = t(T_ETM); r.ae = t(T_AE); r.dUroe = t(T_DUROE); r.dProe = t(T_DPROE); r.dUr = t(T_DUR);
+        r.sub = (__ldg(&tp.flags[e]) & 4) != 0;
+        roe_rev(wL, wR, fL, fR, nx, ny, len, g, r, mu, bwL, bwR, bfL, bfR);
+    } else {
+        llf_rev(fL, fR, wL, wR, nx, ny, len, g, mu, bwL, bwR, bfL, bfR);
+    }
     to_prim_vjp(fR, wR, g, bwR, bfR);
     if (e >= m.E_int) {  // a boundary edge: the ghost is a function of the L face state
         const int bt = __ldg(&m.e_bc[e]);
@@ -99,10 +104,15 @@ __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView
 // ---- per cell: gather face-state adjoints, then limiter + LSQ VJP ---------------
 // The limiter's choices and the gradient before it come from the stage's record
 // (grad_cell<1, true, true>); nothing of the forward is recomputed.
-template <bool LINEAR, bool BARTH>
+// GRAD 1: least squares, the transpose goes to the neighbour differences (bdU); GRAD 2:
+// Green-Gauss, phi_f = g_C U_c + (1 - g_C) U_F on faces with a cell F beyond them (U_c on the
+// others), grad = (1/vol) sum phi_f S_f: the U_c part joins lam_dir, the U_F parts go to bgg
+// (one per face), and the limiter's bound adjoints still go to bdU.
+template <bool LINEAR, bool BARTH, int GRAD>
 __global__ void __launch_bounds__(256) k_adj_cell(MeshView m, const d4* __restrict__ aL, const d4* __restrict__ aR,
                                                   const int* __restrict__ aflag, CellTape ct,
-                                                  d4* __restrict__ lam_dir, d4* __restrict__ bdU) {
+                                                  d4* __restrict__ lam_dir, d4* __restrict__ bdU,
+                                                  d4* __restrict__ bgg) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
     double lu[4] = {0, 0, 0, 0}, lgx[4] = {0, 0, 0, 0}, lgy[4] = {0, 0, 0, 0};
@@ -126,8 +136,8 @@ __global__ void __launch_bounds__(256) k_adj_cell(MeshView m, const d4* __restri
             }
         }
     }
-    lam_dir[c] = mk4(lu[0], lu[1], lu[2], lu[3]);
     double bd[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
+    double bgx_all[4] = {0, 0, 0, 0}, bgy_all[4] = {0, 0, 0, 0};  // adjoint of the unlimited gradient
     if (LINEAR) {
         const int nnb = __ldg(&m.c_nnb[c]);
         const double* B = &m.c_lsq[(size_t)c * 6];
@@ -177,11 +187,34 @@ __global__ void __launch_bounds__(256) k_adj_cell(MeshView m, const d4* __restri
                 for (int k = 0; k < 3; k++)
                     if (k == kk) bd[k][v] += b_num;
             }
+            if (GRAD == 1) {
 #pragma unroll
-            for (int k = 0; k < 3; k++)
-                if (k < nnb) bd[k][v] = fma(b0[k], bgx, fma(b1[k], bgy, bd[k][v]));
+                for (int k = 0; k < 3; k++)
+                    if (k < nnb) bd[k][v] = fma(b0[k], bgx, fma(b1[k], bgy, bd[k][v]));
+            }
+            bgx_all[v] = bgx;
+            bgy_all[v] = bgy;
+        }
+        if (GRAD == 2) {
+            const double* W = &m.c_gg[(size_t)c * 12];
+            const double ginv = __ldg(&m.c_ginv[c]);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const int out = __ldg(&m.c_ggout[c * 3 + j]);
+                const double gC = __ldg(&W[4 * j]), gC1 = __ldg(&W[4 * j + 1]);
+                const double Sx = __ldg(&W[4 * j + 2]), Sy = __ldg(&W[4 * j + 3]);
+                double bf[4];
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const double b_phif = ginv * (Sx * bgx_all[v] + Sy * bgy_all[v]);
+                    lu[v] += out >= 0 ? gC * b_phif : b_phif;
+                    bf[v] = out >= 0 ? gC1 * b_phif : 0.0;
+                }
+                bgg[(size_t)c * 3 + j] = mk4(bf[0], bf[1], bf[2], bf[3]);
+            }
         }
     }
+    lam_dir[c] = mk4(lu[0], lu[1], lu[2], lu[3]);
     for (int k = 0; k < 3; k++) bdU[(size_t)c * 3 + k] = mk4(bd[k][0], bd[k][1], bd[k][2], bd[k][3]);
 }
 
@@ -197,7 +230,8 @@ __global__ void __launch_bounds__(256) k_adj_combine(MeshView m, const int* __re
                                                      const d4* __restrict__ lam_s, const d4* __restrict__ R_s,
                                                      const double* __restrict__ dt_p, double a, double b, double ci,
                                                      int acc_mode, d4* __restrict__ lam_in, d4* __restrict__ acc0,
-                                                     int linear, double* __restrict__ dot_part) {
+                                                     int linear, double* __restrict__ dot_part,
+                                                     const int* __restrict__ ggrev, const d4* __restrict__ bgg) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     double dot = 0.0;
     if (c < m.N) {
@@ -211,6 +245,14 @@ __global__ void __launch_bounds__(256) k_adj_combine(MeshView m, const int* __re
                 const int q = __ldg(&m.c_nbr[c * 3 + k]);
                 const d4 other = ld4(&bdU[(size_t)q * 3 + __ldg(&rev[c * 3 + k])]);  // c is a neighbour of q
                 r[0] += other.x; r[1] += other.y; r[2] += other.z; r[3] += other.w;
+            }
+            if (bgg) {  // Green-Gauss: c is the cell beyond face ggrev[c][k] of its k-th face cell
+                for (int k = 0; k < 3; k++) {
+                    const int q = __ldg(&m.c_ggout[c * 3 + k]);
+                    if (q < 0) continue;
+                    const d4 o = ld4(&bgg[(size_t)q * 3 + __ldg(&ggrev[c * 3 + k])]);
+                    r[0] += o.x; r[1] += o.y; r[2] += o.z; r[3] += o.w;
+                }
             }
         }
         const double dt = *dt_p;
@@ -388,6 +430,8 @@ struct Adjoint {
     int* d_seg_cstar = nullptr;    // per step: the minimising cell
     d4 *d_lam = nullptr, *d_lam_in = nullptr, *d_acc0 = nullptr, *d_aL = nullptr, *d_aR = nullptr;
     d4 *d_k_a2 = nullptr, *d_k_a1 = nullptr, *d_k_seed = nullptr;  // Kutta RK3: lam_U2, lam_U1, a seed
+    d4* d_bgg = nullptr;    // Green-Gauss: per face, the adjoint of the cell beyond it
+    int* d_ggrev = nullptr; // Green-Gauss: the matching face of the cell beyond
     d4 *d_lamdir = nullptr, *d_bdU = nullptr, *d_keepU = nullptr;
     int *d_rlist = nullptr, *d_rev = nullptr;
     double* d_dotp = nullptr;
@@ -412,11 +456,9 @@ struct Adjoint {
         const fvgb_params& p = s->p;
         if (p.equation != 1) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers the Euler equations");
         if (p.steady) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers time-accurate runs (time.is_steady = 0)");
-        if (p.flux_scheme != 2002) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers the Roe flux");
+        if (p.flux_scheme != 2001 && p.flux_scheme != 2002) return fail(FVGB_ERR_ARG, "invalid flux scheme");
         if (p.time_advance != 3101 && p.time_advance != 3103 && p.time_advance != 3104)
             return fail(FVGB_ERR_ARG, "invalid time_advance");
-        if (p.reconstruct == 3002 && p.gradient != 1)
-            return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers least-squares gradients");
         for (int e = s->L.E_int; e < s->E; e++) {
             const int bt = s->L.e_bc[e];
             if (bt != 6001 && bt != 6021 && bt != 6011 && bt != 6012 && bt != 6013)
@@ -477,6 +519,29 @@ struct Adjoint {
         if (p.time_advance == 3103 &&
             ((rc = alloc(d_k_a2, N)) || (rc = alloc(d_k_a1, N)) || (rc = alloc(d_k_seed, N))))
             return rc;
+        if (p.reconstruct == 3002 && p.gradient == 2) {
+            // ggrev[c][k]: the face of cell q = ggout[c][k] whose far cell is c; where c and q
+            // share several faces (tiny periodic meshes), the m-th such face of c is paired with
+            // the m-th of q
+            std::vector<int> ggrev((size_t)3 * N, 0);
+            const std::vector<int>& go = s->L.c_ggout;
+            for (int c = 0; c < N; c++)
+                for (int k = 0; k < 3; k++) {
+                    const int q = go[(size_t)c * 3 + k];
+                    if (q < 0) continue;
+                    int m = 0;
+                    for (int k2 = 0; k2 < k; k2++) m += go[(size_t)c * 3 + k2] == q;
+                    int j = 0;
+                    for (; j < 3; j++)
+                        if (go[(size_t)q * 3 + j] == c && m-- == 0) break;
+                    if (j == 3) return fail(FVGB_ERR_MESH, "Green-Gauss face cells are not mutual");
+                    ggrev[(size_t)c * 3 + k] = j;
+                }
+            if ((rc = alloc(d_ggrev, 3 * (size_t)N)) || (rc = alloc(d_bgg, 3 * (size_t)N))) return rc;
+            AK(cudaMemcpyAsync(d_ggrev, ggrev.data(), sizeof(int) * 3 * (size_t)N, cudaMemcpyHostToDevice,
+                               s->stream));
+            AK(cudaStreamSynchronize(s->stream));
+        }
         return 0;
     }
 
@@ -536,14 +601,28 @@ struct Adjoint {
         const bool linear = v.p.reconstruct == 3002;
         const int nbE = nblk(v.E, dev::kEdgeThreads), nbN = nblk(v.N, 256);
         double* dp = d_dotp + (size_t)dot_slot * nbN;
-        dev::k_adj_edge<<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, v.bc, seed, d_rlist, d_aL, d_aR);
+        if (v.p.flux_scheme == 2002)
+            dev::k_adj_edge<dev::FLUX_ROE><<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, v.bc, seed, d_rlist,
+                                                                              d_aL, d_aR);
+        else
+            dev::k_adj_edge<dev::FLUX_LLF><<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, v.bc, seed, d_rlist,
+                                                                              d_aL, d_aR);
         const int* fl = tape.flags;
-        if (!linear) dev::k_adj_cell<false, false><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU);
-        else if (v.p.limiter == 1)
-            dev::k_adj_cell<true, true><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU);
-        else dev::k_adj_cell<true, false><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU);
+        const bool gg = linear && v.p.gradient == 2;
+#define FVGB_ADJ_CELL(LIN, BAR, GR) \
+    dev::k_adj_cell<LIN, BAR, GR><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU, d_bgg)
+        if (!linear) FVGB_ADJ_CELL(false, false, 1);
+        else if (v.p.limiter == 1) {
+            if (gg) FVGB_ADJ_CELL(true, true, 2);
+            else FVGB_ADJ_CELL(true, true, 1);
+        } else {
+            if (gg) FVGB_ADJ_CELL(true, false, 2);
+            else FVGB_ADJ_CELL(true, false, 1);
+        }
+#undef FVGB_ADJ_CELL
         dev::k_adj_combine<<<nbN, 256, 0, st>>>(v.mv, d_rev, d_lamdir, d_bdU, seed, Rs, dt_p, a, b, ci, acc_mode,
-                                                out, d_acc0, linear ? 1 : 0, dp);
+                                                out, d_acc0, linear ? 1 : 0, dp, gg ? d_ggrev : nullptr,
+                                                gg ? d_bgg : nullptr);
         AK(cudaGetLastError());
         return 0;
     }

@@ -192,6 +192,45 @@ __device__ __forceinline__ void ghost_slip_vjp(const d4 UL, const Prim& wL, doub
     bwL.v += b_unL * ny - b_utL * nx;
 }
 
+// adjoint of llf_flux (physics.cuh; LocalLaxFriedrichs.cpp:4-47): bF -> adjoints of the two
+// primitive face states (bL, bR, 1/rho in .ir) and of the conserved ones (bUL, bUR), all four
+// overwritten.  The flux is rebuilt from the face states; max(aL, aR) passes its adjoint to the
+// side dmax chose.
+__device__ __forceinline__ void llf_rev(const d4 UL, const d4 UR, const Prim& L, const Prim& R, double nx, double ny,
+                                        double length, const Gas& g, const d4 bF, Prim& bL, Prim& bR, d4& bUL,
+                                        d4& bUR) {
+    const double unL = fma(nx, L.u, ny * L.v), unR = fma(nx, R.u, ny * R.v);
+    const double ruL = fma(nx, UL.y, ny * UL.z), ruR = fma(nx, UR.y, ny * UR.z);
+    const double hl = (UL.w + L.p) * L.ir, hr = (UR.w + R.p) * R.ir;
+    const double sL = sqrt(g.gamma * L.p * L.ir), sR = sqrt(g.gamma * R.p * R.ir);
+    const double aL = fabs(unL) + sL, aR = fabs(unR) + sR;
+    const double lm = dmax(aL, aR);
+    const double h = 0.5 * length;
+    const d4 m = mk4(h * bF.x, h * bF.y, h * bF.z, h * bF.w);
+    const double b_lm = -(m.x * (UR.x - UL.x) + m.y * (UR.y - UL.y) + m.z * (UR.z - UL.z) + m.w * (UR.w - UL.w));
+    bUL = mk4(lm * m.x, lm * m.y, lm * m.z, lm * m.w);
+    bUR = mk4(-lm * m.x, -lm * m.y, -lm * m.z, -lm * m.w);
+    const double b_ruL = m.x + m.y * L.u + m.z * L.v + m.w * hl;
+    const double b_ruR = m.x + m.y * R.u + m.z * R.v + m.w * hr;
+    bL = Prim{0, m.y * ruL, m.z * ruL, nx * m.y + ny * m.z, 0};
+    bR = Prim{0, m.y * ruR, m.z * ruR, nx * m.y + ny * m.z, 0};
+    // h = (rho E + p) / rho
+    const double b_hl = m.w * ruL, b_hr = m.w * ruR;
+    bUL.w += b_hl * L.ir; bL.p += b_hl * L.ir; bL.ir += b_hl * (UL.w + L.p);
+    bUR.w += b_hr * R.ir; bR.p += b_hr * R.ir; bR.ir += b_hr * (UR.w + R.p);
+    // ru = n . (rho u)
+    bUL.y += nx * b_ruL; bUL.z += ny * b_ruL;
+    bUR.y += nx * b_ruR; bUR.z += ny * b_ruR;
+    // lm = max(aL, aR), a = |un| + sqrt(gamma p / rho)
+    const bool right = dlt(aL, aR);
+    const double b_aL = right ? 0.0 : b_lm, b_aR = right ? b_lm : 0.0;
+    const double b_unL = b_aL * sgn(unL), b_unR = b_aR * sgn(unR);
+    bL.u += nx * b_unL; bL.v += ny * b_unL;
+    bR.u += nx * b_unR; bR.v += ny * b_unR;
+    if (sL > 0) { bL.p += b_aL * g.gamma * L.ir / (2.0 * sL); bL.ir += b_aL * g.gamma * L.p / (2.0 * sL); }
+    if (sR > 0) { bR.p += b_aR * g.gamma * R.ir / (2.0 * sR); bR.ir += b_aR * g.gamma * R.p / (2.0 * sR); }
+}
+
 // adjoint of ghost_farfield (physics.cuh; get_UR_farField, FVMR/src/space/Flux.cpp:81-163):
 // bUR, the adjoint of the ghost's conserved state, onto the interior face state's primitive
 // variables (bw; .ir carries the 1/rho the sound speed reads).  The branch is re-evaluated

@@ -163,7 +163,7 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
             gy[v] = ginv * sy[v];
         }
     }
-    static_assert(!REC || (GRAD == 1 && BARTH), "the adjoint's record covers least squares with the Barth limiter");
+    static_assert(!REC || BARTH, "the adjoint's record covers the Barth limiter");
     double gxr[4], gyr[4], phiv[4] = {1, 1, 1, 1}, rdv[4] = {0, 0, 0, 0};
     int code = 0;
     if constexpr (REC) {
@@ -315,6 +315,32 @@ __device__ __forceinline__ void tape_put(const EdgeTape& t, int e, const Prim& L
     t.flags[e] = flags | (r.sub ? 4 : 0);
 }
 
+// the tape entry of an LLF edge: the two face states only (the reverse rebuilds the rest)
+__device__ __forceinline__ void tape_put_faces(const EdgeTape& t, int e, const Prim& L, const Prim& R, const d4 UL,
+                                               const d4 UR, int flags) {
+    const size_t E = (size_t)t.E;
+    double* v = t.v;
+    const double vals[T_RUL] = {L.r, L.u, L.v, L.p, L.ir, R.r, R.u, R.v, R.p, R.ir, UL.y, UL.z, UL.w, UR.y, UR.z, UR.w};
+#pragma unroll
+    for (int f = 0; f < T_RUL; f++) v[(size_t)f * E + e] = vals[f];
+    t.flags[e] = flags;
+}
+
+// the flux of a recorded edge and its tape entry
+template <int FLUX>
+__device__ __forceinline__ d4 flux_rec(const Prim& wL, const Prim& wR, const d4 fL, const d4 fR, double nx, double ny,
+                                       double len, const Gas& g, const EdgeTape& tape, int e, int flags) {
+    if constexpr (FLUX == FLUX_ROE) {
+        RoeRec r;
+        const d4 F = roe_core<true>(wL, wR, fL, fR, nx, ny, len, g, &r);
+        tape_put(tape, e, wL, wR, fL, fR, r, flags);
+        return F;
+    } else {
+        tape_put_faces(tape, e, wL, wR, fL, fR, flags);
+        return llf_flux(fL, fR, wL, wR, nx, ny, len, g);
+    }
+}
+
 // an interior or periodic edge (R reconstructed at the partner's midpoint for periodic ones);
 // with REC (Roe, Euler) the edge's tape entry is written as well
 template <int FLUX, bool LINEAR, bool NS, bool REC = false>
@@ -336,7 +362,7 @@ __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, c
     Prim wL, wR;
     d4 fL, fR;
     if constexpr (REC) {
-        static_assert(!REC || (FLUX == FLUX_ROE && !NS), "the adjoint's tape covers the Roe flux of the Euler equations");
+        static_assert(!REC || !NS, "the adjoint's tape covers the Euler equations");
         bool usedL = false, usedR = false;
         double dLx = 0, dLy = 0, dRx = 0, dRy = 0;
         if (LINEAR) {
@@ -345,9 +371,7 @@ __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, c
         }
         fL = face_state_used<LINEAR>(uL, gxL, gyL, dLx, dLy, g, wL, usedL);
         fR = face_state_used<LINEAR>(uR, gxR, gyR, dRx, dRy, g, wR, usedR);
-        RoeRec r;
-        F[e] = roe_core<true>(wL, wR, fL, fR, nx, ny, len, g, &r);
-        tape_put(tape, e, wL, wR, fL, fR, r, (usedL ? 1 : 0) | (usedR ? 2 : 0));
+        F[e] = flux_rec<FLUX>(wL, wR, fL, fR, nx, ny, len, g, tape, e, (usedL ? 1 : 0) | (usedR ? 2 : 0));
         return;
     }
     if (LINEAR) {
@@ -404,7 +428,7 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
     Prim wL;
     if constexpr (REC) {
         if (bt == 6001 || bt == 6021 || bt == 6011 || bt == 6012 || bt == 6013) {
-        static_assert(!REC || (FLUX == FLUX_ROE && !NS), "the adjoint's tape covers the Roe flux of the Euler equations");
+        static_assert(!REC || !NS, "the adjoint's tape covers the Euler equations");
         bool usedL = false;
         const d4 fL = face_state_used<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL, usedL);
         d4 fR;
@@ -417,9 +441,7 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
             if (!ok) atomicAdd(&st->farfield_oor, 1ull);
         }
         const Prim wR = to_prim(fR, g);
-        RoeRec r;
-        F[e] = roe_core<true>(wL, wR, fL, fR, nx, ny, len, g, &r);
-        tape_put(tape, e, wL, wR, fL, fR, r, usedL ? 1 : 0);
+        F[e] = flux_rec<FLUX>(wL, wR, fL, fR, nx, ny, len, g, tape, e, usedL ? 1 : 0);
         return;
         }
     }

@@ -232,8 +232,9 @@ void launch_grad(cudaStream_t s, int gradient, bool barth, const d4* U, const Me
     if (m.N <= 0) return;
     const int b = blocks(m.N, 256);
     const CellTape none;
-    if (tape && tape->gx && gradient == 1 && barth) {  // the adjoint's recorded forward
-        k_grad<1, true, true><<<b, 256, 0, s>>>(U, m, Gx, Gy, *tape);
+    if (tape && tape->gx && barth) {  // the adjoint's recorded forward
+        if (gradient == 1) k_grad<1, true, true><<<b, 256, 0, s>>>(U, m, Gx, Gy, *tape);
+        else k_grad<2, true, true><<<b, 256, 0, s>>>(U, m, Gx, Gy, *tape);
     } else if (gradient == 1) {
         if (barth) k_grad<1, true, false><<<b, 256, 0, s>>>(U, m, Gx, Gy, none);
         else k_grad<1, false, false><<<b, 256, 0, s>>>(U, m, Gx, Gy, none);
@@ -256,9 +257,14 @@ static void flux_impl(cudaStream_t s, const d4* U, const d4* Gx, const d4* Gy, c
 void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, const d4* Gx,
                  const d4* Gy, const MeshView& m, const Gas& g, const BcData& bc, d4* F, Status* st,
                  const EdgeTape* tape) {
-    if (tape && tape->v) {  // the adjoint's recorded forward: Roe, Euler equations only
-        if (linear) flux_impl<FLUX_ROE, true, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
-        else flux_impl<FLUX_ROE, false, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
+    if (tape && tape->v) {  // the adjoint's recorded forward: Euler equations only
+        if (scheme == FLUX_ROE) {
+            if (linear) flux_impl<FLUX_ROE, true, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
+            else flux_impl<FLUX_ROE, false, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
+        } else {
+            if (linear) flux_impl<FLUX_LLF, true, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
+            else flux_impl<FLUX_LLF, false, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
+        }
         return;
     }
     if (scheme == FLUX_ROE) {

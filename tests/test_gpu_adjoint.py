@@ -26,15 +26,16 @@ pytestmark = pytest.mark.gpu
 H = 1e-6
 
 
-def setup_case(tmp_path, n=24, jitter=0.2, time_advance=3104, reconstruct=3002, limiter=1, walls=False, CFL=0.8):
+def setup_case(tmp_path, n=24, jitter=0.2, time_advance=3104, reconstruct=3002, limiter=1, walls=False, CFL=0.8,
+               flux=2002, gradient=1):
     su2 = cases.square_mesh(n, jitter=jitter, directory=str(tmp_path))
     if walls:  # periodic left/right, slip walls top and bottom
         text = open(su2).read().replace("MARKER_TAG= periodic_2", "MARKER_TAG= wall")
         su2 = str(tmp_path / f"channel_{n}.su2")
         open(su2, "w").write(text)
-    tp = str(tmp_path / f"adj_{n}_{time_advance}_{reconstruct}_{limiter}_{walls}.toml")
+    tp = str(tmp_path / f"adj_{n}_{time_advance}_{reconstruct}_{limiter}_{walls}_{flux}_{gradient}.toml")
     with open(tp, "w") as f:
-        f.write(cases.toml_text(flux=2002, reconstruct=reconstruct, gradient=1, limiter=limiter,
+        f.write(cases.toml_text(flux=flux, reconstruct=reconstruct, gradient=gradient, limiter=limiter,
                                 time_advance=time_advance, CFL=CFL))
     p = fv.Params.from_toml(tp)
     mesh = fv.Mesh.read_su2(su2, p)
@@ -160,6 +161,17 @@ def test_adjoint_matches_fd_kutta_rk3(tmp_path):
     assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
 
 
+@pytest.mark.parametrize("flux,gradient", [(2001, 1), (2002, 2), (2001, 2)])
+def test_adjoint_llf_and_green_gauss(tmp_path, flux, gradient):
+    """The LLF flux's reverse (llf_rev) and the Green-Gauss gradient's transpose, periodic faces
+    included (the cell beyond a periodic face is its partner's), with the Barth limiter."""
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=16, flux=flux, gradient=gradient)
+    K = 8
+    rho_t = forward(solver, p, Ut0, K)[0]
+    errs, _ = fd_check(solver, p, U0, rho_t, K, 6)
+    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+
+
 def boundary_case(tmp_path, name, text, su2):
     tp = str(tmp_path / f"{name}.toml")
     with open(tp, "w") as f:
@@ -180,7 +192,7 @@ def boundary_case(tmp_path, name, text, su2):
     return p, solver, U0, Ut0
 
 
-@pytest.mark.parametrize("kind", ["cylinder_far_field", "channel_subsonic", "channel_mach2"])
+@pytest.mark.parametrize("kind", ["cylinder_far_field", "channel_subsonic", "channel_mach2", "channel_gg_llf"])
 def test_adjoint_far_field_inlet_outlet(tmp_path, kind):
     """Far-field, inlet and outlet ghosts (ghost_farfield_vjp, all four sub/supersonic
     branches between the three cases), with slip walls and symmetry edges, against central
@@ -196,6 +208,11 @@ def test_adjoint_far_field_inlet_outlet(tmp_path, kind):
     elif kind == "channel_subsonic":
         su2 = cases.channel_mesh(12, jitter=0.2, directory=d)
         text = cases.toml_text(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3103, CFL=0.6,
+                               vortex=(2.5, 7.0, 3.0), inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0),
+                               outlet=(1.0, 1.0, 0.0, 0.9))
+    elif kind == "channel_gg_llf":  # Green-Gauss boundary faces (the cell's own value), LLF
+        su2 = cases.channel_mesh(12, jitter=0.2, directory=d)
+        text = cases.toml_text(flux=2001, reconstruct=3002, gradient=2, limiter=1, time_advance=3103, CFL=0.6,
                                vortex=(2.5, 7.0, 3.0), inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0),
                                outlet=(1.0, 1.0, 0.0, 0.9))
     else:
