@@ -371,14 +371,24 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_figures(flux):
-    """Per-launch DRAM traffic and FP64 instruction counts from the committed ncu summary."""
+def ncu_figures(flux, cells):
+    """Per-launch DRAM traffic and FP64 flop / instruction counts from the committed ncu summary,
+    scaled from the mesh they are quoted on to this run's by the cell count."""
     path = os.path.join(ROOT, "profiles", "ncu_step_kernels.json")
     try:
         with open(path) as f:
-            return json.load(f).get(flux, {})
+            figs = json.load(f).get(flux, {})
     except Exception:
         return {}
+    out = {}
+    for group, f in figs.items():
+        scale = cells / f["scaled_to_cells"] if f.get("scaled_to_cells") else 1.0
+        g = dict(f)
+        for k in ("dram_bytes_per_launch", "fp64_flop_per_launch", "fp64_inst_per_launch"):
+            if g.get(k) is not None:
+                g[k] = g[k] * scale
+        out[group] = g
+    return out
 
 
 def cpu_baseline(tp, su2, N, threads, max_steps, budget_s=30.0):
@@ -490,7 +500,7 @@ def main():
         avg_ms = prof[dom][0] / prof[dom][1]
         peak, peak_kind = measured_peaks()
         achieved = algo[dom] / (avg_ms / 1e3) / 1e9
-        ncu = ncu_figures(args.flux)
+        ncu = ncu_figures(args.flux, N)
         traffic = ncu.get(dom, {}).get("dram_bytes_per_launch")
         stage_ms = (prof["gradient"][0] + prof["flux"][0] + prof["update"][0]) / max(prof["update"][1], 1)
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
