@@ -1,9 +1,9 @@
 // Discrete adjoint of the explicit step (no counterpart in the reference).
 //
 // For U_{n+1} = Step(U_n) (time step, Runge-Kutta stages; forward Euler 3101,
-// Kutta RK3 3103 or SSP-RK3 3104; Euler equations; least-squares or Green-Gauss gradients
-// with or without the Barth limiter; Roe or LLF flux; interior, periodic, slip-wall, symmetry,
-// far-field, inlet and outlet edges) this
+// Kutta RK3 3103 or SSP-RK3 3104; Euler or laminar Navier-Stokes equations; least-squares
+// or Green-Gauss gradients with or without the Barth limiter; Roe or LLF flux; interior,
+// periodic, slip and no-slip wall, symmetry, far-field, inlet and outlet edges) this
 // computes lambda_0 = (dU_K/dU_0)^T lambda_K by reverse sweeps over the steps,
 // each stage's vector-Jacobian product being the hand-written reverse of the
 // forward kernels (adjoint_device.cuh).  The time step's dependence on the
@@ -49,11 +49,17 @@ constexpr int kEdgeThreads = 128;
 // mu = dLoss/dF_e (F_e enters R_L with +1/-vol and, when e is in R's edge list, R_R with
 // -1/-vol), then the flux VJP from the stage's recorded tape: the face states and the
 // Roe intermediates are read, not recomputed
-template <int FLUX>
+// NS: the viscous flux's adjoints of the averaged state and gradients (viscous_vjp), already
+// divided between the two sides (half each; a boundary edge's L side takes all), go to avu,
+// avgx, avgy; Uin, Gx, Gy are the stage's input state and the gradients it read.
+template <int FLUX, bool NS>
 __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView m, Gas g, BcData bc,
                                                            const d4* __restrict__ lam,
                                                            const int* __restrict__ e_rlist, d4* __restrict__ aL,
-                                                           d4* __restrict__ aR) {
+                                                           d4* __restrict__ aR, const d4* __restrict__ Uin,
+                                                           const d4* __restrict__ Gx, const d4* __restrict__ Gy,
+                                                           d4* __restrict__ avu, d4* __restrict__ avgx,
+                                                           d4* __restrict__ avgy) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m.E) return;
     const int L = __ldg(&m.e_L[e]), R = __ldg(&m.e_R[e]);
@@ -88,9 +94,29 @@ __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView
         llf_rev(fL, fR, wL, wR, nx, ny, len, g, mu, bwL, bwR, bfL, bfR);
     }
     to_prim_vjp(fR, wR, g, bwR, bfR);
+    if (NS) {
+        d4 ua = ld4(&Uin[L]), gxa = ld4(&Gx[L]), gya = ld4(&Gy[L]);
+        const bool two = e < m.E_int;
+        if (two) {  // get_U_Gradient_mean / get_U_mean: averages of both sides
+            const d4 ur = ld4(&Uin[R]), gxr = ld4(&Gx[R]), gyr = ld4(&Gy[R]);
+            ua = mk4(0.5 * (ua.x + ur.x), 0.5 * (ua.y + ur.y), 0.5 * (ua.z + ur.z), 0.5 * (ua.w + ur.w));
+            gxa = mk4(0.5 * (gxa.x + gxr.x), 0.5 * (gxa.y + gxr.y), 0.5 * (gxa.z + gxr.z), 0.5 * (gxa.w + gxr.w));
+            gya = mk4(0.5 * (gya.x + gyr.x), 0.5 * (gya.y + gyr.y), 0.5 * (gya.z + gyr.z), 0.5 * (gya.w + gyr.w));
+        }
+        d4 bu, bgx, bgy;
+        viscous_vjp(ua, gxa, gya, nx, ny, len, g, mu, bu, bgx, bgy);
+        const double f = two ? 0.5 : 1.0;
+        avu[e] = mk4(f * bu.x, f * bu.y, f * bu.z, f * bu.w);
+        avgx[e] = mk4(f * bgx.x, f * bgx.y, f * bgx.z, f * bgx.w);
+        avgy[e] = mk4(f * bgy.x, f * bgy.y, f * bgy.z, f * bgy.w);
+    }
     if (e >= m.E_int) {  // a boundary edge: the ghost is a function of the L face state
         const int bt = __ldg(&m.e_bc[e]);
-        if (bt == 6011) ghost_farfield_vjp(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, bfR, bwL);
+        if (bt == 6002) {  // no-slip adiabatic wall (Flux.cpp:73-79): (rho, -rho u or 0, -rho v or 0, rho E)
+            bfL.x += bfR.x;
+            bfL.w += bfR.w;
+            if (!bc.wall_ref) { bfL.y -= bfR.y; bfL.z -= bfR.z; }
+        } else if (bt == 6011) ghost_farfield_vjp(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, bfR, bwL);
         else if (bt == 6012) ghost_farfield_vjp(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, bfR, bwL);
         else if (bt == 6013) ghost_farfield_vjp(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, bfR, bwL);
         else ghost_slip_vjp(fL, wL, nx, ny, bfR, bfL, bwL);  // slip wall, symmetry
@@ -108,11 +134,12 @@ __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView
 // Green-Gauss, phi_f = g_C U_c + (1 - g_C) U_F on faces with a cell F beyond them (U_c on the
 // others), grad = (1/vol) sum phi_f S_f: the U_c part joins lam_dir, the U_F parts go to bgg
 // (one per face), and the limiter's bound adjoints still go to bdU.
-template <bool LINEAR, bool BARTH, int GRAD>
+template <bool LINEAR, bool BARTH, int GRAD, bool NS>
 __global__ void __launch_bounds__(256) k_adj_cell(MeshView m, const d4* __restrict__ aL, const d4* __restrict__ aR,
                                                   const int* __restrict__ aflag, CellTape ct,
                                                   d4* __restrict__ lam_dir, d4* __restrict__ bdU,
-                                                  d4* __restrict__ bgg) {
+                                                  d4* __restrict__ bgg, const d4* __restrict__ avu,
+                                                  const d4* __restrict__ avgx, const d4* __restrict__ avgy) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
     double lu[4] = {0, 0, 0, 0}, lgx[4] = {0, 0, 0, 0}, lgy[4] = {0, 0, 0, 0};
@@ -134,6 +161,12 @@ __global__ void __launch_bounds__(256) k_adj_cell(MeshView m, const d4* __restri
                 lgx[v] = fma(av[v], dx, lgx[v]);
                 lgy[v] = fma(av[v], dy, lgy[v]);
             }
+        }
+        if (NS) {  // the viscous flux read this cell's state and gradients
+            const d4 u = ld4(&avu[e]), x = ld4(&avgx[e]), y = ld4(&avgy[e]);
+            lu[0] += u.x; lu[1] += u.y; lu[2] += u.z; lu[3] += u.w;
+            lgx[0] += x.x; lgx[1] += x.y; lgx[2] += x.z; lgx[3] += x.w;
+            lgy[0] += y.x; lgy[1] += y.y; lgy[2] += y.z; lgy[3] += y.w;
         }
     }
     double bd[3][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
@@ -305,11 +338,12 @@ __global__ void __launch_bounds__(256) k_adj_lincomb(int n, d4* out, double c0, 
 }
 
 // smallest cell index whose CFL vol / alpha equals the step's minimum
-__global__ void __launch_bounds__(256) k_adj_argmin(MeshView m, const double* __restrict__ alpha, double CFL,
+__global__ void __launch_bounds__(256) k_adj_argmin(MeshView m, const double* __restrict__ alpha,
+                                                    const double* __restrict__ alpha_vis, int ns, double CFL,
                                                     const unsigned long long* dtmin, int* out) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
-    const double d = dmin(1e10, dt_cell<false>(c, m, alpha, nullptr, CFL));
+    const double d = dmin(1e10, ns ? dt_cell<true>(c, m, alpha, alpha_vis, CFL) : dt_cell<false>(c, m, alpha, nullptr, CFL));
     if ((unsigned long long)__double_as_longlong(d) == *dtmin) atomicMin(out, c);
 }
 
@@ -320,7 +354,7 @@ constexpr int kDtThreads = 256;
 __global__ void __launch_bounds__(kDtThreads) k_adj_dt(const double* __restrict__ part, int nb, int nstages,
                                                        double b0, double b1, double b2, const d4* __restrict__ U0,
                                                        MeshView m, Gas g, double CFL, const int* cstar,
-                                                       const double* dt_info, d4* lam) {
+                                                       const double* dt_info, d4* lam, int ns, double value_1) {
     __shared__ double red[kDtThreads];
     double lt = 0.0;
     for (int st = 0; st < nstages; st++) {
@@ -353,6 +387,12 @@ __global__ void __launch_bounds__(kDtThreads) k_adj_dt(const double* __restrict_
         const double* gm = &m.e_geom[(size_t)e * 8];
         const double un = w.y * (gm[0] * gm[2]) + w.z * (gm[1] * gm[2]);
         alpha += fabs(un) + sqrt(g.gamma * w.w * rcp(w.x)) * gm[3];
+        if (ns) {  // the viscous spectral radius (k_alpha<true>, dt_cell<true>)
+            const double ir = rcp(w.x);
+            const double T = w.w / g.R * ir;
+            const double mu = g.C1 * (T * sqrt(T)) * rcp(T + 110.4);
+            alpha = fma(2.0 * gm[2] * value_1 * mu * ir, rcp(m.c_vol[c]), alpha);
+        }
     }
     const double vol = m.c_vol[c];
     const double dt = CFL * vol * rcp(alpha);
@@ -381,6 +421,17 @@ __global__ void __launch_bounds__(kDtThreads) k_adj_dt(const double* __restrict_
         bw.u = b_un * nxl;
         bw.v = b_un * nyl;
         bw.p = b_p;
+        if (ns) {  // alpha_vis = 2 L value_1 mu(T) / rho / vol, T = p / (R rho)
+            const double T = w.w / g.R * ir;
+            const double mu = g.C1 * (T * sqrt(T)) * rcp(T + 110.4);
+            const double b_av = b_alpha * rcp(vol);
+            const double k = 2.0 * gm[2] * value_1;
+            const double b_mu = b_av * k * ir;
+            const double b_T = b_mu * mu * (1.5 / T - 1.0 / (T + 110.4));
+            const double b_irv = b_av * k * mu + b_T * w.w / g.R;
+            bw.r -= b_irv * ir * ir;
+            bw.p += b_T * ir / g.R;
+        }
         const double f = (R != -1) ? 0.5 : 1.0;
         Prim bc{f * bw.r, f * bw.u, f * bw.v, f * bw.p, 0.0};
         d4 bu = mk4(0, 0, 0, 0);
@@ -425,7 +476,10 @@ struct Adjoint {
     std::vector<d4*> seg_R;           // per stage of a segment's steps: the residual R(U_in)
     std::vector<double*> seg_tape;    // per stage of a segment's steps: the edge tape (kTapeFields x E)
     std::vector<int*> seg_tflags;
-    std::vector<dev::CellTape> seg_ctape;  // per stage: the limiter record (LSQ + Barth only)
+    std::vector<dev::CellTape> seg_ctape;  // per stage: the limiter record (Barth only)
+    std::vector<d4*> seg_gx, seg_gy;  // per stage (Navier-Stokes): the limited gradients the viscous flux read
+    d4 *d_avu = nullptr, *d_avgx = nullptr, *d_avgy = nullptr;  // per edge: viscous adjoints of U, Gx, Gy
+    const d4 *vis_gx = nullptr, *vis_gy = nullptr;  // the stage in hand's gradients (set by step_vjp)
     double* d_seg_dt = nullptr;    // per step: dt, dt_raw
     int* d_seg_cstar = nullptr;    // per step: the minimising cell
     d4 *d_lam = nullptr, *d_lam_in = nullptr, *d_acc0 = nullptr, *d_aL = nullptr, *d_aR = nullptr;
@@ -454,17 +508,17 @@ struct Adjoint {
     int setup(Solver* solver, int nsteps, int ncheck) {
         s = solver;
         const fvgb_params& p = s->p;
-        if (p.equation != 1) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers the Euler equations");
+        if (p.equation != 1 && p.equation != 2) return fail(FVGB_ERR_ARG, "invalid equation");
         if (p.steady) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers time-accurate runs (time.is_steady = 0)");
         if (p.flux_scheme != 2001 && p.flux_scheme != 2002) return fail(FVGB_ERR_ARG, "invalid flux scheme");
         if (p.time_advance != 3101 && p.time_advance != 3103 && p.time_advance != 3104)
             return fail(FVGB_ERR_ARG, "invalid time_advance");
         for (int e = s->L.E_int; e < s->E; e++) {
             const int bt = s->L.e_bc[e];
-            if (bt != 6001 && bt != 6021 && bt != 6011 && bt != 6012 && bt != 6013)
+            if (bt != 6001 && bt != 6002 && bt != 6021 && bt != 6011 && bt != 6012 && bt != 6013)
                 return fail(FVGB_ERR_UNSUPPORTED,
-                            "the adjoint covers interior, periodic, slip-wall, symmetry, far-field, inlet and "
-                            "outlet edges");
+                            "the adjoint covers interior, periodic, wall, symmetry, far-field, inlet and outlet "
+                            "edges");
         }
         K = nsteps;
         ncheck = std::max(1, std::min(ncheck, K));
@@ -505,7 +559,15 @@ struct Adjoint {
         seg_tflags.assign((size_t)S * nst, nullptr);
         for (size_t i = 0; i < seg_tape.size(); i++)
             if ((rc = alloc(seg_tape[i], (size_t)dev::kTapeFields * E)) || (rc = alloc(seg_tflags[i], E))) return rc;
-        seg_ctape.assign(p.reconstruct == 3002 && p.limiter == 1 ? (size_t)S * nst : 0, dev::CellTape());
+        const bool grads = p.reconstruct == 3002 || p.equation == 2;  // the step computes gradients
+        seg_ctape.assign(grads && p.limiter == 1 ? (size_t)S * nst : 0, dev::CellTape());
+        if (p.equation == 2) {
+            seg_gx.assign((size_t)S * nst, nullptr);
+            seg_gy.assign((size_t)S * nst, nullptr);
+            for (size_t i = 0; i < seg_gx.size(); i++)
+                if ((rc = alloc(seg_gx[i], N)) || (rc = alloc(seg_gy[i], N))) return rc;
+            if ((rc = alloc(d_avu, E)) || (rc = alloc(d_avgx, E)) || (rc = alloc(d_avgy, E))) return rc;
+        }
         for (auto& t : seg_ctape)
             if ((rc = alloc(t.gx, N)) || (rc = alloc(t.gy, N)) || (rc = alloc(t.phi, N)) || (rc = alloc(t.rden, N)) ||
                 (rc = alloc(t.code, N)))
@@ -553,11 +615,11 @@ struct Adjoint {
         AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
         dev::launch_prim(st, v.d_U, v.d_U0, v.d_prim, v.N, v.gas, copy);
         const double value_1 = std::max(4.0 / 3.0, v.p.gamma / v.p.Pr);
-        dev::launch_dt(st, v.d_prim, v.mv, v.gas, value_1, v.p.CFL, false, v.d_alpha, v.d_alpha_vis,
+        dev::launch_dt(st, v.d_prim, v.mv, v.gas, value_1, v.p.CFL, v.p.equation == 2, v.d_alpha, v.d_alpha_vis,
                        &v.d_state->dtmin_bits, v.d_status);
         AK(cudaMemsetAsync(d_seg_cstar + slot, 0x7f, sizeof(int), st));
-        dev::k_adj_argmin<<<nblk(v.N, 256), 256, 0, st>>>(v.mv, v.d_alpha, v.p.CFL, &v.d_state->dtmin_bits,
-                                                          d_seg_cstar + slot);
+        dev::k_adj_argmin<<<nblk(v.N, 256), 256, 0, st>>>(v.mv, v.d_alpha, v.d_alpha_vis, v.p.equation == 2 ? 1 : 0,
+                                                          v.p.CFL, &v.d_state->dtmin_bits, d_seg_cstar + slot);
         dev::launch_dt_final(st, v.d_state, true);
         AK(cudaMemcpyAsync(d_seg_dt + 2 * slot, &v.d_state->dt, sizeof(double), cudaMemcpyDeviceToDevice, st));
         AK(cudaMemcpyAsync(d_seg_dt + 2 * slot + 1, &v.d_state->dt_raw, sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -569,16 +631,23 @@ struct Adjoint {
             v.rec_tape.E = v.E;
             if (!seg_ctape.empty()) v.rec_ctape = seg_ctape[(size_t)slot * nst + si];
             v.enqueue_stage(kind);
+            if (!seg_gx.empty()) {  // the gradients this stage's viscous fluxes read
+                AK(cudaMemcpyAsync(seg_gx[(size_t)slot * nst + si], v.d_Gx, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice,
+                                   st));
+                AK(cudaMemcpyAsync(seg_gy[(size_t)slot * nst + si], v.d_Gy, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice,
+                                   st));
+            }
+            return 0;
         };
         if (v.p.time_advance == 3101) {
-            stage(0, dev::STAGE_EULER);
+            if (int rc = stage(0, dev::STAGE_EULER)) return rc;
         } else {
             const bool kutta = v.p.time_advance == 3103;
-            stage(0, kutta ? dev::STAGE_RK3_1 : dev::STAGE_SSP_1);
+            if (int rc = stage(0, kutta ? dev::STAGE_RK3_1 : dev::STAGE_SSP_1)) return rc;
             AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst + 1], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
-            stage(1, kutta ? dev::STAGE_RK3_2 : dev::STAGE_SSP_2);
+            if (int rc = stage(1, kutta ? dev::STAGE_RK3_2 : dev::STAGE_SSP_2)) return rc;
             AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst + 2], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
-            stage(2, kutta ? dev::STAGE_RK3_3 : dev::STAGE_SSP_3);
+            if (int rc = stage(2, kutta ? dev::STAGE_RK3_3 : dev::STAGE_SSP_3)) return rc;
         }
         v.d_rec_R = nullptr;
         v.rec_tape = dev::EdgeTape();
@@ -598,26 +667,31 @@ struct Adjoint {
         if (!out) out = d_lam_in;
         Solver& v = *s;
         cudaStream_t st = v.stream;
-        const bool linear = v.p.reconstruct == 3002;
+        const bool ns = v.p.equation == 2;
+        const bool linear = v.p.reconstruct == 3002 || ns;  // the step computes (and reads) gradients
         const int nbE = nblk(v.E, dev::kEdgeThreads), nbN = nblk(v.N, 256);
         double* dp = d_dotp + (size_t)dot_slot * nbN;
-        if (v.p.flux_scheme == 2002)
-            dev::k_adj_edge<dev::FLUX_ROE><<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, v.bc, seed, d_rlist,
-                                                                              d_aL, d_aR);
-        else
-            dev::k_adj_edge<dev::FLUX_LLF><<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, v.bc, seed, d_rlist,
-                                                                              d_aL, d_aR);
+#define FVGB_ADJ_EDGE(FL, NSV)                                                                                  \
+    dev::k_adj_edge<FL, NSV><<<nbE, dev::kEdgeThreads, 0, st>>>(tape, v.mv, v.gas, v.bc, seed, d_rlist, d_aL, d_aR, \
+                                                                Uin, vis_gx, vis_gy, d_avu, d_avgx, d_avgy)
+        if (v.p.flux_scheme == 2002) { if (ns) FVGB_ADJ_EDGE(dev::FLUX_ROE, true); else FVGB_ADJ_EDGE(dev::FLUX_ROE, false); }
+        else { if (ns) FVGB_ADJ_EDGE(dev::FLUX_LLF, true); else FVGB_ADJ_EDGE(dev::FLUX_LLF, false); }
+#undef FVGB_ADJ_EDGE
         const int* fl = tape.flags;
         const bool gg = linear && v.p.gradient == 2;
-#define FVGB_ADJ_CELL(LIN, BAR, GR) \
-    dev::k_adj_cell<LIN, BAR, GR><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU, d_bgg)
-        if (!linear) FVGB_ADJ_CELL(false, false, 1);
-        else if (v.p.limiter == 1) {
-            if (gg) FVGB_ADJ_CELL(true, true, 2);
-            else FVGB_ADJ_CELL(true, true, 1);
+#define FVGB_ADJ_CELL(LIN, BAR, GR, NSV)                                                                           \
+    dev::k_adj_cell<LIN, BAR, GR, NSV><<<nbN, 256, 0, st>>>(v.mv, d_aL, d_aR, fl, ct, d_lamdir, d_bdU, d_bgg, d_avu, \
+                                                           d_avgx, d_avgy)
+        if (!linear) FVGB_ADJ_CELL(false, false, 1, false);
+        else if (ns) {
+            if (v.p.limiter == 1) { if (gg) FVGB_ADJ_CELL(true, true, 2, true); else FVGB_ADJ_CELL(true, true, 1, true); }
+            else { if (gg) FVGB_ADJ_CELL(true, false, 2, true); else FVGB_ADJ_CELL(true, false, 1, true); }
+        } else if (v.p.limiter == 1) {
+            if (gg) FVGB_ADJ_CELL(true, true, 2, false);
+            else FVGB_ADJ_CELL(true, true, 1, false);
         } else {
-            if (gg) FVGB_ADJ_CELL(true, false, 2);
-            else FVGB_ADJ_CELL(true, false, 1);
+            if (gg) FVGB_ADJ_CELL(true, false, 2, false);
+            else FVGB_ADJ_CELL(true, false, 1, false);
         }
 #undef FVGB_ADJ_CELL
         dev::k_adj_combine<<<nbN, 256, 0, st>>>(v.mv, d_rev, d_lamdir, d_bdU, seed, Rs, dt_p, a, b, ci, acc_mode,
@@ -637,6 +711,11 @@ struct Adjoint {
         auto ctp = [&](int si) {
             return seg_ctape.empty() ? dev::CellTape() : seg_ctape[(size_t)slot * nst + si];
         };
+        // the stage's recorded gradients for the viscous reverse (Navier-Stokes)
+        auto use = [&](int si) {
+            vis_gx = seg_gx.empty() ? nullptr : seg_gx[(size_t)slot * nst + si];
+            vis_gy = seg_gy.empty() ? nullptr : seg_gy[(size_t)slot * nst + si];
+        };
         auto tp = [&](int si) {
             dev::EdgeTape t;
             t.v = seg_tape[(size_t)slot * nst + si];
@@ -648,6 +727,7 @@ struct Adjoint {
         double b0 = 1.0, b1 = 0.0, b2 = 0.0;  // b_s of the stages in reverse order
         if (v.p.time_advance == 3101) {
             // U1 = U0 + dt R(U0): a = 0, b = 1
+            use(0);
             if ((rc = stage_vjp(seg_states[(size_t)slot], tp(0), ctp(0), R(0), dtp, 0.0, 1.0, 2, 0))) return rc;
             std::swap(d_lam, d_lam_in);
         } else if (v.p.time_advance == 3103) {
@@ -662,14 +742,17 @@ struct Adjoint {
             const d4* U2 = seg_states[(size_t)slot * 3 + 2];
             const int nbk = nblk(v.N, 256);
             // L2 = dt J2^T (L3/6): seed L3, b = 1/6, no identity term
+            use(2);
             if ((rc = stage_vjp(U2, tp(2), ctp(2), R(2), dtp, 0.0, 1.0 / 6.0, 2, 0, d_lam, d_k_a2, 0.0))) return rc;
             dev::k_adj_lincomb<<<nbk, 256, 0, st>>>(v.N, d_k_seed, 2.0 / 3.0, d_lam, 2.0, d_k_a2, 0.0, nullptr, 0.0,
                                                     nullptr);
             // L1 = dt J1^T s2
+            use(1);
             if ((rc = stage_vjp(U1, tp(1), ctp(1), R(1), dtp, 0.0, 1.0, 2, 1, d_k_seed, d_k_a1, 0.0))) return rc;
             dev::k_adj_lincomb<<<nbk, 256, 0, st>>>(v.N, d_k_seed, 1.0 / 6.0, d_lam, -1.0, d_k_a2, 0.5, d_k_a1, 0.0,
                                                     nullptr);
             // dt J0^T s1, then lam_U0
+            use(0);
             if ((rc = stage_vjp(U0, tp(0), ctp(0), R(0), dtp, 0.0, 1.0, 2, 2, d_k_seed, d_lam_in, 0.0))) return rc;
             dev::k_adj_lincomb<<<nbk, 256, 0, st>>>(v.N, d_lam, 1.0, d_lam, 1.0, d_k_a2, 1.0, d_k_a1, 1.0, d_lam_in);
             AK(cudaGetLastError());
@@ -681,12 +764,15 @@ struct Adjoint {
             const d4* U1 = seg_states[(size_t)slot * 3 + 1];
             const d4* U2 = seg_states[(size_t)slot * 3 + 2];
             // U3 = 1/3 U0 + 2/3 (U2 + dt R(U2))
+            use(2);
             if ((rc = stage_vjp(U2, tp(2), ctp(2), R(2), dtp, 1.0 / 3.0, 2.0 / 3.0, 0, 0))) return rc;
             std::swap(d_lam, d_lam_in);
             // U2 = 3/4 U0 + 1/4 (U1 + dt R(U1))
+            use(1);
             if ((rc = stage_vjp(U1, tp(1), ctp(1), R(1), dtp, 0.75, 0.25, 1, 1))) return rc;
             std::swap(d_lam, d_lam_in);
             // U1 = U0 + dt R(U0); U0 also feeds stages 2 and 3 directly (acc0)
+            use(0);
             if ((rc = stage_vjp(U0, tp(0), ctp(0), R(0), dtp, 0.0, 1.0, 3, 2))) return rc;
             std::swap(d_lam, d_lam_in);
             b0 = 2.0 / 3.0;
@@ -694,7 +780,9 @@ struct Adjoint {
             b2 = 1.0;
         }
         dev::k_adj_dt<<<1, dev::kDtThreads, 0, st>>>(d_dotp, nbN, nst, b0, b1, b2, seg_states[(size_t)slot * nst],
-                                                    v.mv, v.gas, v.p.CFL, d_seg_cstar + slot, dtp, d_lam);
+                                                    v.mv, v.gas, v.p.CFL, d_seg_cstar + slot, dtp, d_lam,
+                                                    v.p.equation == 2 ? 1 : 0,
+                                                    std::max(4.0 / 3.0, v.p.gamma / v.p.Pr));
         AK(cudaGetLastError());
         return 0;
     }

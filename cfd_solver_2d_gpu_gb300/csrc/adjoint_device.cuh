@@ -231,6 +231,78 @@ __device__ __forceinline__ void llf_rev(const d4 UL, const d4 UR, const Prim& L,
     if (sR > 0) { bR.p += b_aR * g.gamma * R.ir / (2.0 * sR); bR.ir += b_aR * g.gamma * R.p / (2.0 * sR); }
 }
 
+// adjoint of viscous_flux (physics.cuh): bF -> adjoints of the averaged state U and of the
+// averaged gradients gx, gy (only bF.y, .z, .w matter; the mass flux has no viscous part);
+// the forward's intermediates are recomputed with its operations, then reversed
+__device__ __forceinline__ void viscous_vjp(const d4 U, const d4 gx, const d4 gy, double nx, double ny, double area,
+                                            const Gas& g, const d4 bF, d4& bU, d4& bgx, d4& bgy) {
+    const double ir = rcp(U.x);
+    const double u = U.y * ir, v = U.z * ir, E = U.w * ir;
+    const double dudx = ir * (gx.y - u * gx.x);
+    const double dvdx = ir * (gx.z - v * gx.x);
+    const double dudy = ir * (gy.y - u * gy.x);
+    const double dvdy = ir * (gy.z - v * gy.x);
+    const double dEdx = ir * (gx.w - E * gx.x);
+    const double dEdy = ir * (gy.w - E * gy.x);
+    const double iCv = g.inv_Cv;
+    const double T = iCv * (E - 0.5 * (u * u + v * v));
+    const double dTdx = (dEdx - u * dudx - v * dvdx) * iCv;
+    const double dTdy = (dEdy - u * dudy - v * dvdy) * iCv;
+    const double mu = g.C1 * (T * sqrt(T)) * rcp(T + 110.4);
+    const double div = dudx + dvdy;
+    const double NMD = -2.0 / 3.0;
+    const double txx = mu * fma(NMD, div, 2.0 * dudx);
+    const double tyy = mu * fma(NMD, div, 2.0 * dvdy);
+    const double txy = mu * (dudy + dvdx);
+    const double akmu = g.Cp * (mu * (1.0 / 0.72));
+    // F.y -= (txx nx + txy ny) A; F.z -= (txy nx + tyy ny) A; F.w -= (Phix nx + Phiy ny) A
+    double b_txx = -area * nx * bF.y, b_txy = -area * (ny * bF.y + nx * bF.z), b_tyy = -area * ny * bF.z;
+    const double b_Phix = -area * nx * bF.w, b_Phiy = -area * ny * bF.w;
+    double b_u = 0, b_v = 0, b_E = 0, b_ir = 0, b_mu = 0;
+    // Phix = akmu dTdx + u txx + v txy, Phiy = akmu dTdy + u txy + v tyy
+    const double b_akmu = b_Phix * dTdx + b_Phiy * dTdy;
+    const double b_dTdx = b_Phix * akmu, b_dTdy = b_Phiy * akmu;
+    b_u += b_Phix * txx + b_Phiy * txy;
+    b_v += b_Phix * txy + b_Phiy * tyy;
+    b_txx += b_Phix * u;
+    b_txy += b_Phix * v + b_Phiy * u;
+    b_tyy += b_Phiy * v;
+    b_mu += b_akmu * g.Cp * (1.0 / 0.72);
+    // stresses
+    b_mu += b_txx * fma(NMD, div, 2.0 * dudx) + b_tyy * fma(NMD, div, 2.0 * dvdy) + b_txy * (dudy + dvdx);
+    const double b_div = mu * NMD * (b_txx + b_tyy);
+    double b_dudx = 2.0 * mu * b_txx + b_div, b_dvdy = 2.0 * mu * b_tyy + b_div;
+    double b_dudy = mu * b_txy, b_dvdx = mu * b_txy;
+    // Sutherland: mu = C1 T^1.5 / (T + 110.4)
+    double b_T = b_mu * mu * (1.5 / T - 1.0 / (T + 110.4));
+    // temperature gradients
+    const double b_dEdx = iCv * b_dTdx, b_dEdy = iCv * b_dTdy;
+    b_u -= iCv * (b_dTdx * dudx + b_dTdy * dudy);
+    b_v -= iCv * (b_dTdx * dvdx + b_dTdy * dvdy);
+    b_dudx -= iCv * b_dTdx * u;
+    b_dvdx -= iCv * b_dTdx * v;
+    b_dudy -= iCv * b_dTdy * u;
+    b_dvdy -= iCv * b_dTdy * v;
+    // T = (E - (u^2 + v^2)/2) / Cv
+    b_E += iCv * b_T;
+    b_u -= iCv * b_T * u;
+    b_v -= iCv * b_T * v;
+    // derivatives of u, v, E from the conserved gradients
+    bgx = mk4(0, ir * b_dudx, ir * b_dvdx, ir * b_dEdx);
+    bgy = mk4(0, ir * b_dudy, ir * b_dvdy, ir * b_dEdy);
+    bgx.x = -ir * (b_dudx * u + b_dvdx * v + b_dEdx * E);
+    bgy.x = -ir * (b_dudy * u + b_dvdy * v + b_dEdy * E);
+    b_ir += b_dudx * (gx.y - u * gx.x) + b_dvdx * (gx.z - v * gx.x) + b_dEdx * (gx.w - E * gx.x) +
+            b_dudy * (gy.y - u * gy.x) + b_dvdy * (gy.z - v * gy.x) + b_dEdy * (gy.w - E * gy.x);
+    b_u -= ir * (b_dudx * gx.x + b_dudy * gy.x);
+    b_v -= ir * (b_dvdx * gx.x + b_dvdy * gy.x);
+    b_E -= ir * (b_dEdx * gx.x + b_dEdy * gy.x);
+    // u = rho u / rho, v, E likewise
+    bU = mk4(0, b_u * ir, b_v * ir, b_E * ir);
+    b_ir += b_u * U.y + b_v * U.z + b_E * U.w;
+    bU.x = -b_ir * ir * ir;
+}
+
 // adjoint of ghost_farfield (physics.cuh; get_UR_farField, FVMR/src/space/Flux.cpp:81-163):
 // bUR, the adjoint of the ghost's conserved state, onto the interior face state's primitive
 // variables (bw; .ir carries the 1/rho the sound speed reads).  The branch is re-evaluated

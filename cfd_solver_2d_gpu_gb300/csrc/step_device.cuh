@@ -362,7 +362,6 @@ __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, c
     Prim wL, wR;
     d4 fL, fR;
     if constexpr (REC) {
-        static_assert(!REC || !NS, "the adjoint's tape covers the Euler equations");
         bool usedL = false, usedR = false;
         double dLx = 0, dLy = 0, dRx = 0, dRy = 0;
         if (LINEAR) {
@@ -371,7 +370,14 @@ __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, c
         }
         fL = face_state_used<LINEAR>(uL, gxL, gyL, dLx, dLy, g, wL, usedL);
         fR = face_state_used<LINEAR>(uR, gxR, gyR, dRx, dRy, g, wR, usedR);
-        F[e] = flux_rec<FLUX>(wL, wR, fL, fR, nx, ny, len, g, tape, e, (usedL ? 1 : 0) | (usedR ? 2 : 0));
+        d4 flux = flux_rec<FLUX>(wL, wR, fL, fR, nx, ny, len, g, tape, e, (usedL ? 1 : 0) | (usedR ? 2 : 0));
+        if (NS) {
+            const d4 ua = mk4(0.5 * (uL.x + uR.x), 0.5 * (uL.y + uR.y), 0.5 * (uL.z + uR.z), 0.5 * (uL.w + uR.w));
+            const d4 gxa = mk4(0.5 * (gxL.x + gxR.x), 0.5 * (gxL.y + gxR.y), 0.5 * (gxL.z + gxR.z), 0.5 * (gxL.w + gxR.w));
+            const d4 gya = mk4(0.5 * (gyL.x + gyR.x), 0.5 * (gyL.y + gyR.y), 0.5 * (gyL.z + gyR.z), 0.5 * (gyL.w + gyR.w));
+            viscous_flux(flux, ua, gxa, gya, nx, ny, len, g);
+        }
+        F[e] = flux;
         return;
     }
     if (LINEAR) {
@@ -427,13 +433,14 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
     }
     Prim wL;
     if constexpr (REC) {
-        if (bt == 6001 || bt == 6021 || bt == 6011 || bt == 6012 || bt == 6013) {
-        static_assert(!REC || !NS, "the adjoint's tape covers the Euler equations");
+        if (bt == 6001 || bt == 6021 || bt == 6002 || bt == 6011 || bt == 6012 || bt == 6013) {
         bool usedL = false;
         const d4 fL = face_state_used<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL, usedL);
         d4 fR;
         if (bt == 6001 || bt == 6021) {
             fR = ghost_slip(fL, wL, nx, ny);
+        } else if (bt == 6002) {  // get_UR_wall_adiabat (Flux.cpp:73-79)
+            fR = bc.wall_ref ? mk4(fL.x, -0.0, -0.0, fL.w) : mk4(fL.x, -fL.y, -fL.z, fL.w);
         } else {
             const bool ok = bt == 6011   ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
                             : bt == 6012 ? ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR)
@@ -441,7 +448,9 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
             if (!ok) atomicAdd(&st->farfield_oor, 1ull);
         }
         const Prim wR = to_prim(fR, g);
-        F[e] = flux_rec<FLUX>(wL, wR, fL, fR, nx, ny, len, g, tape, e, usedL ? 1 : 0);
+        d4 flux = flux_rec<FLUX>(wL, wR, fL, fR, nx, ny, len, g, tape, e, usedL ? 1 : 0);
+        if (NS) viscous_flux(flux, uL, gxL, gyL, nx, ny, len, g);  // boundary: the L cell's values
+        F[e] = flux;
         return;
         }
     }

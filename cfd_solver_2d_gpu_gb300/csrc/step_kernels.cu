@@ -257,14 +257,16 @@ static void flux_impl(cudaStream_t s, const d4* U, const d4* Gx, const d4* Gy, c
 void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, const d4* Gx,
                  const d4* Gy, const MeshView& m, const Gas& g, const BcData& bc, d4* F, Status* st,
                  const EdgeTape* tape) {
-    if (tape && tape->v) {  // the adjoint's recorded forward: Euler equations only
+    if (tape && tape->v) {  // the adjoint's recorded forward
+#define FVGB_REC(FL, LIN, NSV) flux_impl<FL, LIN, NSV, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape)
         if (scheme == FLUX_ROE) {
-            if (linear) flux_impl<FLUX_ROE, true, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
-            else flux_impl<FLUX_ROE, false, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
+            if (linear) { if (ns) FVGB_REC(FLUX_ROE, true, true); else FVGB_REC(FLUX_ROE, true, false); }
+            else { if (ns) FVGB_REC(FLUX_ROE, false, true); else FVGB_REC(FLUX_ROE, false, false); }
         } else {
-            if (linear) flux_impl<FLUX_LLF, true, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
-            else flux_impl<FLUX_LLF, false, false, true>(s, U, Gx, Gy, m, g, bc, F, st, *tape);
+            if (linear) { if (ns) FVGB_REC(FLUX_LLF, true, true); else FVGB_REC(FLUX_LLF, true, false); }
+            else { if (ns) FVGB_REC(FLUX_LLF, false, true); else FVGB_REC(FLUX_LLF, false, false); }
         }
+#undef FVGB_REC
         return;
     }
     if (scheme == FLUX_ROE) {

@@ -226,3 +226,31 @@ def test_adjoint_far_field_inlet_outlet(tmp_path, kind):
     errs, g = fd_check(solver, p, U0, rho_t, K, 6)
     assert np.all(np.isfinite(g))
     assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+
+
+@pytest.mark.parametrize("kind", ["vortex_ns", "channel_ns_gg", "channel_ns_o1_mirror"])
+def test_adjoint_navier_stokes(tmp_path, kind):
+    """The laminar viscous flux's reverse (viscous_vjp: the averaged state and the gradients it
+    reads, through the gradient and limiter transposes), the no-slip wall's ghost in both of
+    its forms, and the viscous term of the time step, at Re = 100."""
+    d = str(tmp_path)
+    if kind == "vortex_ns":  # periodic, LSQ + Barth, Roe, SSP-RK3
+        su2 = cases.square_mesh(16, jitter=0.2, directory=d)
+        text = cases.toml_text(equation=2, flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104,
+                               CFL=0.6, Re=100.0)
+    elif kind == "channel_ns_gg":  # no-slip wall (the reference's ghost), symmetry, inlet, outlet
+        su2 = cases.channel_mesh(12, jitter=0.2, directory=d)
+        text = cases.toml_text(equation=2, flux=2002, reconstruct=3002, gradient=2, limiter=1, time_advance=3103,
+                               CFL=0.6, Re=100.0, vortex=(2.5, 7.0, 3.0), inf=(1.0, 1.0, 0.3, 1.0),
+                               inlet=(1.0, 1.0, 0.3, 1.0), outlet=(1.0, 1.0, 0.0, 0.9))
+    else:  # constant reconstruction (the viscous flux still reads gradients), mirrored wall ghost, LLF
+        su2 = cases.channel_mesh(12, jitter=0.2, directory=d)
+        text = cases.toml_text(equation=2, flux=2001, reconstruct=3001, gradient=1, limiter=1, time_advance=3101,
+                               CFL=0.5, Re=100.0, vortex=(2.5, 7.0, 3.0), inf=(1.0, 1.0, 0.3, 1.0),
+                               inlet=(1.0, 1.0, 0.3, 1.0), outlet=(1.0, 1.0, 0.0, 0.9), wall_bc="mirror")
+    p, solver, U0, Ut0 = boundary_case(tmp_path, kind, text, su2)
+    K = 6
+    rho_t = forward(solver, p, Ut0, K)[0]
+    errs, g = fd_check(solver, p, U0, rho_t, K, 6)
+    assert np.all(np.isfinite(g))
+    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
