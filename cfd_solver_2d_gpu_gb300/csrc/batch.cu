@@ -43,15 +43,15 @@ namespace {
         if (e_ != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-StageFn pick(int kind, int flux, bool linear, int grad, bool barth) {
+StageFn pick(int kind, int flux, bool linear, int grad, bool barth, bool ns) {
     switch (kind) {
-    case dev::STAGE_EULER: return batch_stage_euler(flux, linear, grad, barth);
-    case dev::STAGE_RK3_1: return batch_stage_rk3_1(flux, linear, grad, barth);
-    case dev::STAGE_RK3_2: return batch_stage_rk3_2(flux, linear, grad, barth);
-    case dev::STAGE_RK3_3: return batch_stage_rk3_3(flux, linear, grad, barth);
-    case dev::STAGE_SSP_1: return batch_stage_ssp_1(flux, linear, grad, barth);
-    case dev::STAGE_SSP_2: return batch_stage_ssp_2(flux, linear, grad, barth);
-    default: return batch_stage_ssp_3(flux, linear, grad, barth);
+    case dev::STAGE_EULER: return batch_stage_euler(flux, linear, grad, barth, ns);
+    case dev::STAGE_RK3_1: return batch_stage_rk3_1(flux, linear, grad, barth, ns);
+    case dev::STAGE_RK3_2: return batch_stage_rk3_2(flux, linear, grad, barth, ns);
+    case dev::STAGE_RK3_3: return batch_stage_rk3_3(flux, linear, grad, barth, ns);
+    case dev::STAGE_SSP_1: return batch_stage_ssp_1(flux, linear, grad, barth, ns);
+    case dev::STAGE_SSP_2: return batch_stage_ssp_2(flux, linear, grad, barth, ns);
+    default: return batch_stage_ssp_3(flux, linear, grad, barth, ns);
     }
 }
 
@@ -102,7 +102,9 @@ struct Batch {
         return 0;
     }
 
-    StageFn fn(int kind) const { return pick(kind, p.flux_scheme, p.reconstruct == 3002, p.gradient, p.limiter == 1); }
+    StageFn fn(int kind) const {
+        return pick(kind, p.flux_scheme, p.reconstruct == 3002, p.gradient, p.limiter == 1, p.equation == 2);
+    }
 
     int launch(int kind) {
         StageFn f = fn(kind);
@@ -292,7 +294,10 @@ struct Batch {
                 q.restrict_ref != p.restrict_ref)
                 return fail(FVGB_ERR_ARG, "batched instances must share the scheme and the gas constants");
         }
-        if (p.equation != 1) return fail(FVGB_ERR_UNSUPPORTED, "the batched form runs the Euler equations");
+        if (p.equation == 2)  // one Gas for the launch: the viscosity law and Pr are shared too
+            for (int i = 0; i < n; i++)
+                if (params[i].mu0 != p.mu0 || params[i].T0 != p.T0 || params[i].Pr != p.Pr)
+                    return fail(FVGB_ERR_ARG, "batched Navier-Stokes instances must share mu0, T0 and Pr");
         for (int i = 0; i < n; i++)
             if (params[i].steady)
                 return fail(FVGB_ERR_UNSUPPORTED, "the batched form steps in time (time.is_steady = 0)");

@@ -102,7 +102,7 @@ __device__ __forceinline__ void for_tiles(const BatchView& bv, int n, int phase,
     }
 }
 
-template <int KIND, int FLUX, bool LINEAR, bool GRADIENT, int GRAD, bool BARTH>
+template <int KIND, int FLUX, bool LINEAR, bool GRADIENT, int GRAD, bool BARTH, bool NS>
 __global__ void k_batch_stage(BatchView bv, Gas g) {
     const MeshView& m = bv.m;
     constexpr bool FIRST = (KIND == STAGE_EULER || KIND == STAGE_RK3_1 || KIND == STAGE_SSP_1);
@@ -115,7 +115,7 @@ __global__ void k_batch_stage(BatchView bv, Gas g) {
         const bool copy = KIND != STAGE_EULER;
         for_tiles(bv, m.N, 0, [&](int c) { prim_cell(c, bv.U, bv.U0, bv.prim, g, copy); });
         if (!grid_sync(bv.bar)) return;
-        for_tiles(bv, m.E, 1, [&](int e) { alpha_edge<false>(e, bv.prim, m, g, bv.value_1, bv.alpha, bv.alpha_vis, bv.status); });
+        for_tiles(bv, m.E, 1, [&](int e) { alpha_edge<NS>(e, bv.prim, m, g, bv.value_1, bv.alpha, bv.alpha_vis, bv.status); });
         if (!grid_sync(bv.bar)) return;
         // per-instance minimum: segmented warp reduction over contiguous cells of one instance
         const int ntiles = (m.N + bv.tile - 1) / bv.tile;
@@ -125,7 +125,7 @@ __global__ void k_batch_stage(BatchView bv, Gas g) {
                 const int c = base + threadIdx.x;
                 const bool live = c < end;
                 const int inst = live ? __ldg(&bv.c_inst[c]) : -1;
-                double v = live ? dt_cell<false>(c, m, bv.alpha, bv.alpha_vis, bv.inst[inst].CFL) : 1e10;
+                double v = live ? dt_cell<NS>(c, m, bv.alpha, bv.alpha_vis, bv.inst[inst].CFL) : 1e10;
                 const int lane = threadIdx.x & 31;
                 for (int o = 1; o < 32; o <<= 1) {
                     const double v2 = __shfl_down_sync(0xffffffffu, v, o);
@@ -160,11 +160,11 @@ __global__ void k_batch_stage(BatchView bv, Gas g) {
     }
     for_tiles(bv, m.E, 3, [&](int e) {
         if (e < m.E_int) {
-            flux_interior<FLUX, LINEAR, false>(e, bv.U, bv.Gx, bv.Gy, m, g, bv.F);
+            flux_interior<FLUX, LINEAR, NS>(e, bv.U, bv.Gx, bv.Gy, m, g, bv.F);
         } else {
             BcData bc = bv.bc[__ldg(&bv.e_inst[e])];
             bc.clock_frac = dsr_stage_frac(KIND);
-            flux_boundary<FLUX, LINEAR, false>(e, bv.U, bv.Gx, bv.Gy, m, g, bc, bv.F, bv.status);
+            flux_boundary<FLUX, LINEAR, NS>(e, bv.U, bv.Gx, bv.Gy, m, g, bc, bv.F, bv.status);
         }
     });
     if (!grid_sync(bv.bar)) return;
@@ -186,34 +186,43 @@ __global__ void k_batch_stage(BatchView bv, Gas g) {
 namespace batch_detail {
 using StageFn = void (*)(dev::BatchView, dev::Gas);
 
-template <int KIND, int FLUX, bool LINEAR, bool GRADIENT, int GRAD, bool BARTH>
+template <int KIND, int FLUX, bool LINEAR, bool GRADIENT, int GRAD, bool BARTH, bool NS>
 inline StageFn stage_ptr() {
-    return dev::k_batch_stage<KIND, FLUX, LINEAR, GRADIENT, GRAD, BARTH>;
+    return dev::k_batch_stage<KIND, FLUX, LINEAR, GRADIENT, GRAD, BARTH, NS>;
+}
+
+// the gradient variants of one flux: with linear reconstruction, and (Navier-Stokes only) with
+// constant reconstruction, whose viscous fluxes still read gradients
+template <int KIND, int FLUX, bool NS>
+inline StageFn pick_grad(bool linear, int grad, bool barth) {
+    if (linear) {
+        if (grad == 1) return barth ? stage_ptr<KIND, FLUX, true, true, 1, true, NS>() : stage_ptr<KIND, FLUX, true, true, 1, false, NS>();
+        return barth ? stage_ptr<KIND, FLUX, true, true, 2, true, NS>() : stage_ptr<KIND, FLUX, true, true, 2, false, NS>();
+    }
+    if constexpr (NS) {
+        if (grad == 1) return barth ? stage_ptr<KIND, FLUX, false, true, 1, true, NS>() : stage_ptr<KIND, FLUX, false, true, 1, false, NS>();
+        return barth ? stage_ptr<KIND, FLUX, false, true, 2, true, NS>() : stage_ptr<KIND, FLUX, false, true, 2, false, NS>();
+    } else {
+        return stage_ptr<KIND, FLUX, false, false, 1, false, false>();
+    }
 }
 
 template <int KIND>
-inline StageFn pick_kind(int flux, bool linear, int grad, bool barth) {
-    if (!linear) {
-        return flux == 2002 ? stage_ptr<KIND, 2002, false, false, 1, false>() : stage_ptr<KIND, 2001, false, false, 1, false>();
-    }
-    if (flux == 2002) {
-        if (grad == 1) return barth ? stage_ptr<KIND, 2002, true, true, 1, true>() : stage_ptr<KIND, 2002, true, true, 1, false>();
-        return barth ? stage_ptr<KIND, 2002, true, true, 2, true>() : stage_ptr<KIND, 2002, true, true, 2, false>();
-    }
-    if (grad == 1) return barth ? stage_ptr<KIND, 2001, true, true, 1, true>() : stage_ptr<KIND, 2001, true, true, 1, false>();
-    return barth ? stage_ptr<KIND, 2001, true, true, 2, true>() : stage_ptr<KIND, 2001, true, true, 2, false>();
+inline StageFn pick_kind(int flux, bool linear, int grad, bool barth, bool ns) {
+    if (flux == 2002) return ns ? pick_grad<KIND, 2002, true>(linear, grad, barth) : pick_grad<KIND, 2002, false>(linear, grad, barth);
+    return ns ? pick_grad<KIND, 2001, true>(linear, grad, barth) : pick_grad<KIND, 2001, false>(linear, grad, barth);
 }
 
 }  // namespace batch_detail
 
 using StageFn = batch_detail::StageFn;
 // one translation unit per stage kind instantiates its kernels (parallel build)
-StageFn batch_stage_euler(int flux, bool linear, int grad, bool barth);
-StageFn batch_stage_rk3_1(int flux, bool linear, int grad, bool barth);
-StageFn batch_stage_rk3_2(int flux, bool linear, int grad, bool barth);
-StageFn batch_stage_rk3_3(int flux, bool linear, int grad, bool barth);
-StageFn batch_stage_ssp_1(int flux, bool linear, int grad, bool barth);
-StageFn batch_stage_ssp_2(int flux, bool linear, int grad, bool barth);
-StageFn batch_stage_ssp_3(int flux, bool linear, int grad, bool barth);
+StageFn batch_stage_euler(int flux, bool linear, int grad, bool barth, bool ns);
+StageFn batch_stage_rk3_1(int flux, bool linear, int grad, bool barth, bool ns);
+StageFn batch_stage_rk3_2(int flux, bool linear, int grad, bool barth, bool ns);
+StageFn batch_stage_rk3_3(int flux, bool linear, int grad, bool barth, bool ns);
+StageFn batch_stage_ssp_1(int flux, bool linear, int grad, bool barth, bool ns);
+StageFn batch_stage_ssp_2(int flux, bool linear, int grad, bool barth, bool ns);
+StageFn batch_stage_ssp_3(int flux, bool linear, int grad, bool barth, bool ns);
 
 }  // namespace fvgb

@@ -273,8 +273,9 @@ void fvgb_adjoint_release(fvgb_handle* h);
 /* ---- batched instances -----------------------------------------------------
  * No counterpart in the reference (one mesh per process, the driver loop of
  * FVMR/src/drivers/CDriver.cpp:75-80 stepping it).  n independent instances of
- * the Euler step (their own meshes, far-field states, CFL, time and end time;
- * one shared scheme) packed into one device layout and advanced by one
+ * the Euler or laminar Navier-Stokes step (their own meshes, far-field states,
+ * CFL, time and end time; one shared scheme and gas, for Navier-Stokes the same
+ * mu0, T0 and Pr) packed into one device layout and advanced by one
  * persistent cooperative kernel per Runge-Kutta stage, the step captured in a
  * CUDA graph.  Each instance gives bit for bit what fvgb_step gives for it
  * alone.  States are in each instance's reference numbering. */

@@ -98,6 +98,22 @@ def test_batch_matches_plain_double_mach_reflection(tmp_path):
         assert t[i] == tp
 
 
+@pytest.mark.parametrize("reconstruct,gradient", [(3002, 1), (3001, 2)])
+def test_batch_matches_plain_navier_stokes(tmp_path, reconstruct, gradient):
+    """Laminar cylinders (no-slip wall, far field; one viscosity law for the batch), second
+    order with least squares, and first order with Green-Gauss gradients for the viscous flux."""
+    inst = cylinders(tmp_path, [6, 9, 12], [0.2, 0.3, 0.45], equation=2, reconstruct=reconstruct, gradient=gradient)
+    b = fv.Batch([m for m, _ in inst], [p for _, p in inst])
+    t = b.step(4)
+    for i, (m, p) in enumerate(inst):
+        U, tp = plain_run(m, p, 4)
+        assert np.array_equal(b.get_state(i), U), i
+        assert t[i] == tp
+    other = cylinders(tmp_path, [5], [0.2], equation=2, mu0=2e-5)[0]
+    with pytest.raises(fv.FvgbError):
+        fv.Batch([inst[0][0], other[0]], [inst[0][1], other[1]])
+
+
 def test_autotuner_keeps_state_and_result(tmp_path):
     inst = cylinders(tmp_path, [8, 14, 5], [0.1, 0.4, 0.6])
     b = fv.Batch([m for m, _ in inst], [p for _, p in inst])
