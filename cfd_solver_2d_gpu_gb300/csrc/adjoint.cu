@@ -3,7 +3,8 @@
 // For U_{n+1} = Step(U_n) (time step, Runge-Kutta stages; forward Euler 3101,
 // Kutta RK3 3103 or SSP-RK3 3104; Euler or laminar Navier-Stokes equations; least-squares
 // or Green-Gauss gradients with or without the Barth limiter; Roe or LLF flux; interior,
-// periodic, slip and no-slip wall, symmetry, far-field, inlet and outlet edges) this
+// periodic, slip and no-slip wall, symmetry, far-field, inlet, outlet and double-Mach-
+// reflection edges) this
 // computes lambda_0 = (dU_K/dU_0)^T lambda_K by reverse sweeps over the steps,
 // each stage's vector-Jacobian product being the hand-written reverse of the
 // forward kernels (adjoint_device.cuh).  The time step's dependence on the
@@ -116,6 +117,9 @@ __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView
             bfL.x += bfR.x;
             bfL.w += bfR.w;
             if (!bc.wall_ref) { bfL.y -= bfR.y; bfL.z -= bfR.z; }
+        } else if (bt == 6014) {  // double Mach reflection: the side the forward took (tape flag bit 3)
+            if (__ldg(&tp.flags[e]) & 8) ghost_farfield_vjp(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, bfR, bwL);
+            else ghost_farfield_vjp(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, bfR, bwL);
         } else if (bt == 6011) ghost_farfield_vjp(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, bfR, bwL);
         else if (bt == 6012) ghost_farfield_vjp(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, bfR, bwL);
         else if (bt == 6013) ghost_farfield_vjp(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, bfR, bwL);
@@ -515,10 +519,8 @@ struct Adjoint {
             return fail(FVGB_ERR_ARG, "invalid time_advance");
         for (int e = s->L.E_int; e < s->E; e++) {
             const int bt = s->L.e_bc[e];
-            if (bt != 6001 && bt != 6002 && bt != 6021 && bt != 6011 && bt != 6012 && bt != 6013)
-                return fail(FVGB_ERR_UNSUPPORTED,
-                            "the adjoint covers interior, periodic, wall, symmetry, far-field, inlet and outlet "
-                            "edges");
+            if (bt != 6001 && bt != 6002 && bt != 6021 && bt != 6011 && bt != 6012 && bt != 6013 && bt != 6014)
+                return fail(FVGB_ERR_UNSUPPORTED, "unknown boundary type");
         }
         K = nsteps;
         ncheck = std::max(1, std::min(ncheck, K));

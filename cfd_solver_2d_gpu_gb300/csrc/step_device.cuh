@@ -433,14 +433,21 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
     }
     Prim wL;
     if constexpr (REC) {
-        if (bt == 6001 || bt == 6021 || bt == 6002 || bt == 6011 || bt == 6012 || bt == 6013) {
+        if (bt == 6001 || bt == 6021 || bt == 6002 || bt == 6011 || bt == 6012 || bt == 6013 || bt == 6014) {
         bool usedL = false;
+        int dsr_flag = 0;  // bit 3: a "dsr" edge took the inlet state
         const d4 fL = face_state_used<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL, usedL);
         d4 fR;
         if (bt == 6001 || bt == 6021) {
             fR = ghost_slip(fL, wL, nx, ny);
         } else if (bt == 6002) {  // get_UR_wall_adiabat (Flux.cpp:73-79)
             fR = bc.wall_ref ? mk4(fL.x, -0.0, -0.0, fL.w) : mk4(fL.x, -fL.y, -fL.z, fL.w);
+        } else if (bt == 6014) {
+            const bool up = dsr_upstream(__ldg(&gm[6]), __ldg(&gm[7]), bc);
+            dsr_flag = up ? 8 : 0;
+            const bool ok = up ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
+                               : ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR);
+            if (!ok) atomicAdd(&st->farfield_oor, 1ull);
         } else {
             const bool ok = bt == 6011   ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
                             : bt == 6012 ? ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR)
@@ -448,7 +455,7 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
             if (!ok) atomicAdd(&st->farfield_oor, 1ull);
         }
         const Prim wR = to_prim(fR, g);
-        d4 flux = flux_rec<FLUX>(wL, wR, fL, fR, nx, ny, len, g, tape, e, usedL ? 1 : 0);
+        d4 flux = flux_rec<FLUX>(wL, wR, fL, fR, nx, ny, len, g, tape, e, (usedL ? 1 : 0) | dsr_flag);
         if (NS) viscous_flux(flux, uL, gxL, gyL, nx, ny, len, g);  // boundary: the L cell's values
         F[e] = flux;
         return;

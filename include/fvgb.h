@@ -257,9 +257,8 @@ int fvgb_output_timed(fvgb_handle* h, int reps, double* ms_node_field, double* m
  * No counterpart in the reference.  Reverse-mode derivative of K steps of the
  * handle's own step map U_0 -> U_K (Euler or laminar Navier-Stokes equations,
  * Roe or LLF flux, least-squares or Green-Gauss gradients with or without the
- * Barth limiter, forward Euler, Kutta RK3 or SSP-RK3, every boundary kind but
- * the double Mach reflection's; the time step's dependence on the state
- * included).  fvgb_adjoint_forward runs the K steps from U0 at time t0
+ * Barth limiter, forward Euler, Kutta RK3 or SSP-RK3, every boundary kind; the
+ * time step's dependence on the state included).  fvgb_adjoint_forward runs the K steps from U0 at time t0
  * keeping n_checkpoints states (sqrt(K) keeps memory at O(sqrt(K) N)) and
  * returns U_K; fvgb_adjoint_backward then maps a seed dL/dU_K to dL/dU_0
  * (both [4][N], reference numbering), recomputing each segment once.  The

@@ -192,7 +192,8 @@ def boundary_case(tmp_path, name, text, su2):
     return p, solver, U0, Ut0
 
 
-@pytest.mark.parametrize("kind", ["cylinder_far_field", "channel_subsonic", "channel_mach2", "channel_gg_llf"])
+@pytest.mark.parametrize("kind", ["cylinder_far_field", "channel_subsonic", "channel_mach2", "channel_gg_llf",
+                                  "channel_dsr"])
 def test_adjoint_far_field_inlet_outlet(tmp_path, kind):
     """Far-field, inlet and outlet ghosts (ghost_farfield_vjp, all four sub/supersonic
     branches between the three cases), with slip walls and symmetry edges, against central
@@ -208,6 +209,13 @@ def test_adjoint_far_field_inlet_outlet(tmp_path, kind):
     elif kind == "channel_subsonic":
         su2 = cases.channel_mesh(12, jitter=0.2, directory=d)
         text = cases.toml_text(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3103, CFL=0.6,
+                               vortex=(2.5, 7.0, 3.0), inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0),
+                               outlet=(1.0, 1.0, 0.0, 0.9))
+    elif kind == "channel_dsr":  # the top boundary as "dsr": inlet state left of the moving shock, outlet right
+        text0 = open(cases.channel_mesh(12, jitter=0.2, directory=d)).read()
+        su2 = str(tmp_path / "channel_dsr.su2")
+        open(su2, "w").write(text0.replace("MARKER_TAG= symmetry", "MARKER_TAG= dsr"))
+        text = cases.toml_text(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.6,
                                vortex=(2.5, 7.0, 3.0), inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0),
                                outlet=(1.0, 1.0, 0.0, 0.9))
     elif kind == "channel_gg_llf":  # Green-Gauss boundary faces (the cell's own value), LLF
