@@ -113,16 +113,16 @@ __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView
     }
     if (e >= m.E_int) {  // a boundary edge: the ghost is a function of the L face state
         const int bt = __ldg(&m.e_bc[e]);
-        if (bt == 6002) {  // no-slip adiabatic wall (Flux.cpp:73-79): (rho, -rho u or 0, -rho v or 0, rho E)
+        if (bt == BC_WALL_ADIABAT) {  // no-slip adiabatic wall (Flux.cpp:73-79): (rho, -rho u or 0, -rho v or 0, rho E)
             bfL.x += bfR.x;
             bfL.w += bfR.w;
             if (!bc.wall_ref) { bfL.y -= bfR.y; bfL.z -= bfR.z; }
-        } else if (bt == 6014) {  // double Mach reflection: the side the forward took (tape flag bit 3)
+        } else if (bt == BC_DSR) {  // double Mach reflection: the side the forward took (tape flag bit 3)
             if (__ldg(&tp.flags[e]) & 8) ghost_farfield_vjp(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, bfR, bwL);
             else ghost_farfield_vjp(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, bfR, bwL);
-        } else if (bt == 6011) ghost_farfield_vjp(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, bfR, bwL);
-        else if (bt == 6012) ghost_farfield_vjp(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, bfR, bwL);
-        else if (bt == 6013) ghost_farfield_vjp(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, bfR, bwL);
+        } else if (bt == BC_INLET) ghost_farfield_vjp(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, bfR, bwL);
+        else if (bt == BC_OUTLET) ghost_farfield_vjp(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, bfR, bwL);
+        else if (bt == BC_INF) ghost_farfield_vjp(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, bfR, bwL);
         else ghost_slip_vjp(fL, wL, nx, ny, bfR, bfL, bwL);  // slip wall, symmetry
         bfR = mk4(0, 0, 0, 0);
     }
@@ -519,7 +519,7 @@ struct Adjoint {
             return fail(FVGB_ERR_ARG, "invalid time_advance");
         for (int e = s->L.E_int; e < s->E; e++) {
             const int bt = s->L.e_bc[e];
-            if (bt != 6001 && bt != 6002 && bt != 6021 && bt != 6011 && bt != 6012 && bt != 6013 && bt != 6014)
+            if (bt != BC_WALL_NONVISCOUS && bt != BC_WALL_ADIABAT && bt != BC_SYMMETRY && bt != BC_INLET && bt != BC_OUTLET && bt != BC_INF && bt != BC_DSR)
                 return fail(FVGB_ERR_UNSUPPORTED, "unknown boundary type");
         }
         K = nsteps;

@@ -4,23 +4,10 @@
 #include <string>
 #include <vector>
 
+#include "bc_types.h"
 #include "fvgb.h"
 
 namespace fvgb {
-
-// boundary type codes, FVMR/src/global/Constexpr.h:47-57
-enum BcType : int {
-    BC_INTERIOR = -1,
-    BC_WALL_NONVISCOUS = 6001,
-    BC_WALL_ADIABAT = 6002,
-    BC_INLET = 6011,
-    BC_OUTLET = 6012,
-    BC_INF = 6013,
-    BC_DSR = 6014,
-    BC_SYMMETRY = 6021,
-    BC_PERIODIC_0 = 6100,
-    BC_PERIODIC_9 = 6109,
-};
 
 // constants of FVMR/src/math/CommonValue.h:16-29
 constexpr double kEps = 1e-10;

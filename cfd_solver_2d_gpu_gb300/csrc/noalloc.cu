@@ -82,17 +82,17 @@ __global__ void __launch_bounds__(256) k_noalloc_flux(RefMesh m, const double* _
     const d4 uL = load_ref(U, m.N, L);
     const dev::Prim wL = dev::to_prim(uL, g);
     d4 uR = mk4(0, 0, 0, 0);
-    if (bt == 6001 || bt == 6021) {
+    if (bt == BC_WALL_NONVISCOUS || bt == BC_SYMMETRY) {
         uR = dev::ghost_slip(uL, wL, nx, ny);
-    } else if (bt == 6002) {
+    } else if (bt == BC_WALL_ADIABAT) {
         uR = bc.wall_ref ? mk4(uL.x, -0.0, -0.0, uL.w) : mk4(uL.x, -uL.y, -uL.z, uL.w);
-    } else if (bt == 6011) {
+    } else if (bt == BC_INLET) {
         dev::ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, uR);
-    } else if (bt == 6012) {
+    } else if (bt == BC_OUTLET) {
         dev::ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, uR);
-    } else if (bt == 6013) {
+    } else if (bt == BC_INF) {
         dev::ghost_farfield(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, uR);
-    } else if (bt == 6014) {
+    } else if (bt == BC_DSR) {
         if (dev::dsr_upstream_at(m.edge_xy[e], m.edge_xy[(size_t)m.E + e], t_dsr, bc))
             dev::ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, uR);
         else

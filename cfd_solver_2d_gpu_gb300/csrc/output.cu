@@ -283,7 +283,7 @@ static void forces(const Solver& s, double* cd, double* cl, double* cd_wall, dou
         if (cd) cd[b] = CD;
         if (cl) cl[b] = CL;
         const int t = s.om.set_type[b];
-        if (t == BC_WALL_NONVISCOUS || t == BC_WALL_ADIABAT || t == 6003) {  // set_CDCL_wall: the wall types
+        if (t == BC_WALL_NONVISCOUS || t == BC_WALL_ADIABAT || t == BC_WALL_ISOTHERMAL) {  // set_CDCL_wall: the wall types
             dw += CD;
             lw += CL;
         }

@@ -10,6 +10,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "bc_types.h"
+
 namespace fvgb {
 
 // cell state (rho, rho u, rho v, rho E): 32-byte aligned so one state is one sector

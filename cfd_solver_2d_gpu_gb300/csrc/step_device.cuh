@@ -433,24 +433,24 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
     }
     Prim wL;
     if constexpr (REC) {
-        if (bt == 6001 || bt == 6021 || bt == 6002 || bt == 6011 || bt == 6012 || bt == 6013 || bt == 6014) {
+        if (bt == BC_WALL_NONVISCOUS || bt == BC_SYMMETRY || bt == BC_WALL_ADIABAT || bt == BC_INLET || bt == BC_OUTLET || bt == BC_INF || bt == BC_DSR) {
         bool usedL = false;
         int dsr_flag = 0;  // bit 3: a "dsr" edge took the inlet state
         const d4 fL = face_state_used<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL, usedL);
         d4 fR;
-        if (bt == 6001 || bt == 6021) {
+        if (bt == BC_WALL_NONVISCOUS || bt == BC_SYMMETRY) {
             fR = ghost_slip(fL, wL, nx, ny);
-        } else if (bt == 6002) {  // get_UR_wall_adiabat (Flux.cpp:73-79)
+        } else if (bt == BC_WALL_ADIABAT) {  // get_UR_wall_adiabat (Flux.cpp:73-79)
             fR = bc.wall_ref ? mk4(fL.x, -0.0, -0.0, fL.w) : mk4(fL.x, -fL.y, -fL.z, fL.w);
-        } else if (bt == 6014) {
+        } else if (bt == BC_DSR) {
             const bool up = dsr_upstream(__ldg(&gm[6]), __ldg(&gm[7]), bc);
             dsr_flag = up ? 8 : 0;
             const bool ok = up ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
                                : ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR);
             if (!ok) atomicAdd(&st->farfield_oor, 1ull);
         } else {
-            const bool ok = bt == 6011   ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
-                            : bt == 6012 ? ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR)
+            const bool ok = bt == BC_INLET   ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
+                            : bt == BC_OUTLET ? ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR)
                                          : ghost_farfield(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, fR);
             if (!ok) atomicAdd(&st->farfield_oor, 1ull);
         }
@@ -464,23 +464,23 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
     const d4 fL = face_state<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL);
     d4 fR = mk4(0, 0, 0, 0);
     switch (bt) {
-    case 6021:  // symmetry
-    case 6001:  // slip wall, get_UR_wallNonViscous
+    case BC_SYMMETRY:  // symmetry
+    case BC_WALL_NONVISCOUS:  // slip wall, get_UR_wallNonViscous
         fR = ghost_slip(fL, wL, nx, ny);
         break;
-    case 6002:  // no-slip adiabatic wall, get_UR_wall_adiabat (Flux.cpp:73-79)
+    case BC_WALL_ADIABAT:  // no-slip adiabatic wall, get_UR_wall_adiabat (Flux.cpp:73-79)
         fR = bc.wall_ref ? mk4(fL.x, -0.0, -0.0, fL.w) : mk4(fL.x, -fL.y, -fL.z, fL.w);
         break;
-    case 6011:
+    case BC_INLET:
         if (!ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
         break;
-    case 6012:
+    case BC_OUTLET:
         if (!ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
         break;
-    case 6013:
+    case BC_INF:
         if (!ghost_farfield(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
         break;
-    case 6014: {  // boundary edges keep their midpoint in the slots of the absent R offset
+    case BC_DSR: {  // boundary edges keep their midpoint in the slots of the absent R offset
         const bool up = dsr_upstream(__ldg(&gm[6]), __ldg(&gm[7]), bc);
         const bool ok = up ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
                            : ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR);
