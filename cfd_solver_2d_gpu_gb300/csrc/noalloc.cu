@@ -53,7 +53,7 @@ int scratch_address(int device, double** out) {
 }
 
 struct RefMesh {  // device pointers, reference layout and numbering
-    int N, E;
+    int N, E, NB;
     const int* elem_edges;   // [4][N]
     const double* elem_volume;
     const int* edge_L;
@@ -76,7 +76,14 @@ __global__ void __launch_bounds__(256) k_noalloc_flux(RefMesh m, const double* _
                                                       dev::BcData bc, double t_dsr, double* __restrict__ F) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m.E) return;
-    const int L = m.edge_L[e], R = m.edge_R[e], set = m.edge_setID[e];
+    const int L = m.edge_L[e], set = m.edge_setID[e];
+    int R = m.edge_R[e];
+    // indices outside the caller's arrays are not followed: such an edge's flux is NaN
+    if (L < 0 || L >= m.N || R < -1 || R >= m.N || (set != -1 && (set < 1 || set > m.NB))) {
+        const double nan = __longlong_as_double(0x7ff8000000000000LL);
+        for (int v = 0; v < 4; v++) F[(size_t)v * m.E + e] = nan;
+        return;
+    }
     const int bt = set != -1 ? m.boundary_type[set - 1] : -1;
     const double nx = m.edge_normal[e], ny = m.edge_normal[(size_t)m.E + e], len = m.edge_length[e];
     const d4 uL = load_ref(U, m.N, L);
@@ -141,6 +148,14 @@ extern "C" int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params
     if (p->reconstruct != 3001 || p->equation != 1)
         return fail(FVGB_ERR_UNSUPPORTED, "fvgb_rhs_noalloc: constant reconstruction (3001) and Euler (1) only");
     if (p->flux_scheme != 2001 && p->flux_scheme != 2002) return fail(FVGB_ERR_ARG, "invalid flux scheme");
+    {  // every array the kernels may read must be there (a null device address would fault)
+        const fvgb_mesh_soa& d = *dev_mesh;
+        const bool e = d.num_edge > 0, n = d.num_element > 0;
+        if ((n && (!d.elem_edges || !d.elem_volume)) ||
+            (e && (!d.edge_L || !d.edge_R || !d.edge_setID || !d.edge_length || !d.edge_normal || !d.edge_xy)) ||
+            (e && !d.boundary_type))
+            return fail(FVGB_ERR_ARG, "fvgb_rhs_noalloc: a mesh array it reads is NULL");
+    }
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess) return fail(FVGB_ERR_CUDA, cudaGetErrorString(e));
@@ -149,6 +164,7 @@ extern "C" int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params
     if (rc) return rc;
     RefMesh m;
     m.N = dev_mesh->num_element;
+    m.NB = dev_mesh->num_boundary;
     m.E = dev_mesh->num_edge;
     m.elem_edges = dev_mesh->elem_edges;
     m.elem_volume = dev_mesh->elem_volume;

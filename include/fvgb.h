@@ -309,8 +309,8 @@ int fvgb_batch_info(fvgb_batch* b, long long out[8]);
  * device or pinned memory: for callers that already manage every GPU buffer
  * themselves and may not add allocations of their own.  dev_mesh holds DEVICE
  * pointers to the reference-layout arrays (elem_edges, elem_volume, edge_L,
- * edge_R, edge_setID, edge_length, edge_normal, boundary_type are read, and
- * edge_xy where a "dsr" boundary exists: its edges are evaluated at p->dsr_time);
+ * edge_R, edge_setID, edge_length, edge_normal, edge_xy and boundary_type
+ * are read, none may be NULL; "dsr" edges are evaluated at p->dsr_time);
  * U_dev is U[4][N] and rhs_dev receives RHS[4][N] = -(1/vol) sum of edge
  * fluxes, both on the device; stream is a cudaStream_t (NULL = default
  * stream); the call only enqueues work.  The edge fluxes are kept in one

@@ -203,3 +203,20 @@ def test_steady_inputs(tmp_path):
     with pytest.raises(fv.FvgbError) as e:
         fv.Batch([m], [p])
     assert "is_steady" in str(e.value)
+
+
+def test_rhs_noalloc_refuses_null_mesh_arrays():
+    """fvgb_rhs_noalloc reads the caller's device arrays; a NULL among them is refused on the
+    host before anything is launched (no GPU needed to see it)."""
+    L = fv.lib()
+    L.fvgb_rhs_noalloc.restype = ctypes.c_int
+    L.fvgb_rhs_noalloc.argtypes = [ctypes.POINTER(fv.MeshSoA), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p]
+    p = fv.Params.default()
+    p.reconstruct, p.equation, p.flux_scheme = 3001, 1, 2002
+    soa = fv.MeshSoA()
+    soa.num_element, soa.num_edge, soa.num_boundary = 4, 6, 1
+    dummy = ctypes.c_double()
+    rc = L.fvgb_rhs_noalloc(ctypes.byref(soa), ctypes.addressof(p), ctypes.addressof(dummy), ctypes.addressof(dummy),
+                            None)
+    assert rc == -1 and "NULL" in L.fvgb_last_error().decode()
