@@ -34,9 +34,44 @@ uint64_t spread(uint32_t x) {
     return v;
 }
 bool is_periodic(int t) { return t >= BC_PERIODIC_0 && t <= BC_PERIODIC_9; }
+
+// The caller's arrays are checked before anything indexes them, so that a bad
+// index is an error code rather than a host crash or an out-of-bounds gather on
+// the device (every device index is derived from these).
+int validate_mesh(const fvgb_mesh_soa& m) {
+    const int N = m.num_element, E = m.num_edge, V = m.num_node, NB = m.num_boundary;
+    if (N < 0 || E < 0 || V < 0 || NB < 0) return fail(FVGB_ERR_MESH, "negative mesh sizes");
+    if ((N > 0 && (!m.elem_edges || !m.elem_nodes || !m.elem_neighbors || !m.elem_xy || !m.elem_volume)) ||
+        (E > 0 && (!m.edge_L || !m.edge_R || !m.edge_setID || !m.edge_periodicPair || !m.edge_length ||
+                   !m.edge_xy || !m.edge_normal || !m.edge_nodes)) ||
+        (V > 0 && !m.node_xy) || (NB > 0 && !m.boundary_type))
+        return fail(FVGB_ERR_MESH, "a mesh array is NULL");
+    auto in = [](int x, int lo, int hi) { return x >= lo && x < hi; };
+    for (int e = 0; e < E; e++) {
+        const int s = m.edge_setID[e];
+        if (!in(m.edge_L[e], 0, N) || !in(m.edge_R[e], -1, N) || !(s == -1 || in(s, 1, NB + 1)) ||
+            !in(m.edge_periodicPair[e], -1, E) || !in(m.edge_nodes[e], 0, V) ||
+            !in(m.edge_nodes[(size_t)E + e], 0, V))
+            return fail(FVGB_ERR_MESH, "edge " + std::to_string(e) + " refers outside the mesh");
+    }
+    for (int c = 0; c < N; c++)
+        for (int j = 0; j < 3; j++)
+            if (!in(m.elem_edges[(size_t)j * N + c], 0, E) || !in(m.elem_nodes[(size_t)j * N + c], 0, V) ||
+                !in(m.elem_neighbors[(size_t)j * N + c], -1, N))
+                return fail(FVGB_ERR_MESH, "cell " + std::to_string(c) + " refers outside the mesh");
+    if (m.set_edge_offsets && m.set_edge_list) {
+        if (m.set_edge_offsets[0] != 0) return fail(FVGB_ERR_MESH, "boundary set offsets do not start at 0");
+        for (int b = 0; b < NB; b++)
+            if (m.set_edge_offsets[b + 1] < m.set_edge_offsets[b]) return fail(FVGB_ERR_MESH, "boundary set offsets decrease");
+        for (int i = 0; i < (NB > 0 ? m.set_edge_offsets[NB] : 0); i++)
+            if (!in(m.set_edge_list[i], 0, E)) return fail(FVGB_ERR_MESH, "boundary set edge outside the mesh");
+    }
+    return 0;
+}
 }  // namespace
 
 int build_layout(const fvgb_mesh_soa& m, const fvgb_params& p, Layout& L) {
+    if (int rc = validate_mesh(m)) return rc;
     const int N = m.num_element, E = m.num_edge, V = m.num_node;
     L = Layout();
     L.N = N;

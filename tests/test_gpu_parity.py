@@ -207,3 +207,22 @@ def test_pinned_host_buffers_match_pageable(tmp_path):
     out = torch.empty((4, m.N), dtype=torch.float64).pin_memory()
     b.get_state_ptr(out.data_ptr())
     assert np.array_equal(a.get_state(), out.numpy())
+
+
+def test_bad_mesh_indices_are_refused(tmp_path):
+    """Indices outside the caller's arrays (an edge's cell, a cell's edge, a boundary set) are
+    refused with FVGB_ERR_MESH before anything is built or launched."""
+    import ctypes
+    su2 = cases.square_mesh(6, jitter=0.2, directory=str(tmp_path))
+    p = fv.Params.default()
+    m = fv.Mesh.read_su2(su2, p)
+    for name, index, value in (("edge_L", 3, m.N), ("edge_R", 0, -2), ("edge_setID", m.E - 1, m.NB + 1),
+                               ("elem_edges", 5, m.E)):
+        arr = np.ascontiguousarray(m.array(name)).copy()
+        arr.reshape(-1)[index] = value
+        soa = fv.MeshSoA()
+        ctypes.memmove(ctypes.byref(soa), ctypes.byref(m.soa), ctypes.sizeof(soa))
+        setattr(soa, name, arr.ctypes.data)
+        h = ctypes.c_void_p()
+        rc = fv.lib().fvgb_create(ctypes.byref(soa), ctypes.byref(p), ctypes.byref(h))
+        assert rc == -4 and "outside" in fv.lib().fvgb_last_error().decode(), name
