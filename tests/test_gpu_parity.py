@@ -213,8 +213,8 @@ def test_bad_mesh_indices_are_refused(tmp_path):
     """Indices outside the caller's arrays (an edge's cell, a cell's edge, a boundary set) are
     refused with FVGB_ERR_MESH before anything is built or launched."""
     import ctypes
-    su2 = cases.square_mesh(6, jitter=0.2, directory=str(tmp_path))
-    p = fv.Params.default()
+    tp, su2 = cases.vortex_small(str(tmp_path), n=6)
+    p = fv.Params.from_toml(tp)
     m = fv.Mesh.read_su2(su2, p)
     for name, index, value in (("edge_L", 3, m.N), ("edge_R", 0, -2), ("edge_setID", m.E - 1, m.NB + 1),
                                ("elem_edges", 5, m.E)):
