@@ -226,3 +226,25 @@ def test_bad_mesh_indices_are_refused(tmp_path):
         h = ctypes.c_void_p()
         rc = fv.lib().fvgb_create(ctypes.byref(soa), ctypes.byref(p), ctypes.byref(h))
         assert rc == -4 and "outside" in fv.lib().fvgb_last_error().decode(), name
+
+
+@pytest.mark.parametrize("kind", ["square2", "square3", "channel2"])
+@pytest.mark.parametrize("second_order", [False, True])
+def test_tiny_meshes_match_the_oracle(tmp_path, kind, second_order):
+    """The smallest meshes the writers make: 8 and 18 triangles on the periodic square (a
+    cell's periodic faces wrap onto cells it also meets inside) and the 8-triangle channel,
+    every cell of which touches a boundary."""
+    n = int(kind[-1])
+    su2 = (cases.square_mesh if kind.startswith("square") else cases.channel_mesh)(n, directory=str(tmp_path))
+    tp = str(tmp_path / "tiny.toml")
+    with open(tp, "w") as f:
+        f.write(cases.toml_text(flux=2002, reconstruct=3002 if second_order else 3001, gradient=1, limiter=1,
+                                time_advance=3104, CFL=0.5))
+    s, p, m = make(tp, su2)
+    o = Oracle(tp, su2)
+    U0 = cases.wavy(m, o.init_field())
+    s.set_state(U0)
+    s.step(0.0, p.T_end, 4)
+    o.params.time_advance = 3104
+    Uo, _, _, _ = o.run(U0, 4)
+    assert rel(s.get_state(), Uo) <= 1e-12
