@@ -227,7 +227,7 @@ class RunConfig(ctypes.Structure):
                 ("start_output_field", ctypes.c_int), ("max_iteration", ctypes.c_int),
                 ("tolerance_residual", ctypes.c_double), ("filename", ctypes.c_char * 256),
                 ("mesh_file_type", ctypes.c_char * 16), ("volume_preset", ctypes.c_int),
-                ("boundary_preset", ctypes.c_int)]
+                ("boundary_preset", ctypes.c_int), ("time_strategy", ctypes.c_int)]
 
 
 def run_config(path):

@@ -39,6 +39,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -130,6 +131,10 @@ int main(int argc, char** argv) {
 
     fvgb_handle* h = nullptr;
     if (fvgb_create(&soa, &p, &h)) return report("fvgb_create");
+    // time.strategy: the adaptive CFL of RoutineController, applied at each print event
+    fvgb_cfl_controller* ctl_raw = nullptr;
+    if (fvgb_cfl_controller_create(rc.time_strategy, &ctl_raw)) return report("time.strategy");
+    std::unique_ptr<fvgb_cfl_controller, void (*)(fvgb_cfl_controller*)> ctl(ctl_raw, fvgb_cfl_controller_destroy);
     if (fvgb_set_state(h, U.data())) return report("fvgb_set_state");
 
     // write_tecplot_hist_file: the head when the file is new or the run did not restart
@@ -186,6 +191,16 @@ int main(int argc, char** argv) {
         const bool write_hist = istep == 1 || istep % rc.step_per_output_hist == 0;
         const bool write_field =
             istep == 1 || (istep % rc.step_per_output_field == 0 && istep >= rc.start_output_field);
+        if (print) {  // CDriver.cpp:115-125: the residual, then the CFL strategy, then the print
+            int applied = 0;
+            double cfl = p.CFL;
+            if (fvgb_cfl_controller_apply(ctl.get(), res[0], istep, &cfl, &applied)) return report("time.strategy");
+            if (applied && cfl != p.CFL) {
+                p.CFL = cfl;
+                if (fvgb_set_cfl(h, cfl)) return report("fvgb_set_cfl");
+                if (!quiet) std::printf("step = %d\tresidual_rho = %.6e\tCFL = %.9g\n", istep, res[0], cfl);
+            }
+        }
         if (print && !quiet)
             std::printf("step = %d\tt = %.9g\tresidual_rho = %.6e\tresidual_rhou = %.6e\tresidual_rhov = %.6e\t"
                         "residual_rhoE = %.6e\n",

@@ -396,6 +396,10 @@ extern "C" int fvgb_run_config_read_toml(const char* path, fvgb_run_config* c) {
     r.num("output.tolerace_residual", c->tolerance_residual, false);
     r.integer("output.outputScheme_volume_preset", c->volume_preset, false);
     r.integer("output.outputScheme_boundary_preset", c->boundary_preset, false);
+    c->time_strategy = 0;
+    r.integer("time.strategy", c->time_strategy, false);  // TomlFileManager.cpp:154-156
+    if (c->time_strategy != 0 && c->time_strategy != 1)   // CInput.cpp:53-54
+        return fail(FVGB_ERR_FORMAT, "input.toml: time.strategy is 0 (none) or 1 (adaptive CFL)");
     if (c->volume_preset < 0 || c->volume_preset > 2 || c->boundary_preset < 0 || c->boundary_preset > 2)
         return fail(FVGB_ERR_FORMAT, "input.toml: output scheme presets are 0, 1 or 2");
     if (!r.missing.empty()) return fail(FVGB_ERR_FORMAT, "input.toml: wrong type for" + r.missing);

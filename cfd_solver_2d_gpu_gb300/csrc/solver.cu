@@ -532,6 +532,20 @@ extern "C" int fvgb_set_time(fvgb_handle* h, double t) {
     return h->s.set_time(t);
 }
 
+extern "C" int fvgb_set_cfl(fvgb_handle* h, double CFL) {
+    GUARD(h);
+    if (!(CFL > 0.0)) return fail(FVGB_ERR_ARG, "CFL must be positive");
+    Solver& s = h->s;
+    if (s.p.CFL == CFL) return 0;
+    CK(cudaStreamSynchronize(s.stream));  // no launch of the old graph is still pending
+    s.p.CFL = CFL;
+    if (s.graph_exec) {  // the step was captured with the old value
+        cudaGraphExecDestroy(s.graph_exec);
+        s.graph_exec = nullptr;
+    }
+    return 0;
+}
+
 extern "C" int fvgb_time(fvgb_handle* h, double* t, double* last_dt) {
     GUARD(h);
     return h->s.get_time(t, last_dt);

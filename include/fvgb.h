@@ -131,8 +131,21 @@ typedef struct fvgb_run_config {
     char mesh_file_type[16];     /* basic.meshFileType */
     int volume_preset;           /* output.outputScheme_volume_preset: 0 rho u v p, 1 + Cp, 2 + Ma (default 2) */
     int boundary_preset;         /* output.outputScheme_boundary_preset (default 1) */
+    int time_strategy;           /* time.strategy: 0 none, 1 adaptive CFL (RoutineController) */
 } fvgb_run_config;
 int fvgb_run_config_read_toml(const char* path, fvgb_run_config* c);
+/* The driver's adaptive CFL, RoutineController (FVMR/src/drivers/RoutineController.cpp:
+ * 13-90) as CDriver::start applies it at each print event with the residual of rho
+ * (CDriver.cpp:115-120): strategy 0 leaves CFL alone; strategy 1 records the first
+ * residual, then (after step 1000) scales CFL by 0.75 when the residual exceeds ten
+ * times the record, and (after step 5000) by 1.1 when it falls below half the
+ * record (the record then x 0.9) and by 1.05 otherwise, each change with its
+ * cool-down (500 / 1000 steps), CFL never below 0.5.  *applied = 1 when CFL
+ * changed; pass the new value to fvgb_set_cfl. */
+typedef struct fvgb_cfl_controller fvgb_cfl_controller;
+int fvgb_cfl_controller_create(int strategy, fvgb_cfl_controller** out);
+int fvgb_cfl_controller_apply(fvgb_cfl_controller* c, double residual_rho, int step, double* CFL, int* applied);
+void fvgb_cfl_controller_destroy(fvgb_cfl_controller* c);
 /* Reads and assembles an .su2 mesh with the reference's numbering
  * (SU2MeshReader::read_mesh_and_process, FVMR/src/input/SU2MeshReader.cpp:10-251,
  * FVM_2D::iniEdges.., FVMR/src/legacy/FVM_2D.cpp:36-198) in O(N). */
@@ -183,6 +196,10 @@ int fvgb_step(fvgb_handle* h, double* t, double T, int nsteps);
 int fvgb_step_async(fvgb_handle* h, double T, int nsteps);
 int fvgb_set_time(fvgb_handle* h, double t);
 int fvgb_time(fvgb_handle* h, double* t, double* last_dt);
+/* changes the CFL number of the following steps (GlobalPara::time::CFL, which the
+ * reference's driver adjusts through RoutineController, CDriver.cpp:115-120); the
+ * captured step is rebuilt at the next fvgb_step.  CFL must be positive. */
+int fvgb_set_cfl(fvgb_handle* h, double CFL);
 int fvgb_synchronize(fvgb_handle* h);
 /* calculateFunctionF on a given state (FVMR/src/time/Evolve.cpp:98-112):
  * rhs[4][N]; grad_x/grad_y[4][N] (limited gradients) may be NULL. */

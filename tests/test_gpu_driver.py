@@ -3,6 +3,7 @@ gives the same state as stepping through the C ABI directly, a run stopped and
 restarted from its pause file ends bit for bit where an unbroken run ends, and a
 NaN ends the run with status 2 and a nan_ continue file (as CDriver::start's
 signal packs, FVMR/src/drivers/CDriver.cpp:202-263)."""
+import ctypes
 import os
 import shutil
 import subprocess
@@ -88,3 +89,35 @@ def test_nan_stops_with_status_2(tmp_path):
     r = run(make_case(d, 20, cont=True), out)
     assert r.returncode == 2, (r.returncode, r.stdout, r.stderr)
     assert any(f.startswith("nan_jv[") for f in os.listdir(out))
+
+
+def test_driver_adaptive_cfl(tmp_path):
+    """time.strategy = 1: past step 5000 the driver raises CFL at its print events as
+    RoutineController does (x 1.1 or x 1.05 with a 1000-step cool-down); the steps after a
+    change equal a solver created with the new CFL, and the pause file keeps it."""
+    d = str(tmp_path / "case")
+    os.makedirs(d)
+    text = cases.toml_text(flux=2002, reconstruct=3001, gradient=1, limiter=1, time_advance=3101, CFL=0.5,
+                           filename="sq", max_iteration=5060)
+    text = text.replace("[time]\n", "[time]\nstrategy = 1\n").replace(
+        "step_per_output_field = 100", "step_per_output_field = 100000")
+    tp = os.path.join(d, "input.toml")
+    with open(tp, "w") as f:
+        f.write(text)
+    shutil.copy(cases.square_mesh(8), os.path.join(d, "sq.su2"))
+    r = run(tp, os.path.join(d, "out"))
+    assert r.returncode == 0, r.stderr
+    changes = [l for l in r.stdout.split("\n") if "CFL = " in l]
+    assert len(changes) == 1 and changes[0].startswith("step = 5050"), changes
+    new = float(changes[0].split("CFL = ")[1])
+    assert new in (0.5 * 1.1, 0.5 * 1.05)
+    _, U, t, istep, cfl = fv.Mesh.read_continue(os.path.join(d, "out", "pause_sq[5060].dat"))
+    assert istep == 5060 and cfl == new
+    # the same run through the C ABI: 5050 steps at 0.5, then 10 at the new CFL
+    p = fv.Params.from_toml(tp)
+    m = fv.Mesh.read_su2(os.path.join(d, "sq.su2"), p)
+    s = fv.GPUSolver2(m, p)
+    t1 = s.step(0.0, p.T_end, 5050)
+    assert fv.lib().fvgb_set_cfl(s._h, ctypes.c_double(new)) == 0
+    t2 = s.step(t1, p.T_end, 10)
+    assert np.array_equal(s.get_state(), U) and t2 == t

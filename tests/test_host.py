@@ -220,3 +220,82 @@ def test_rhs_noalloc_refuses_null_mesh_arrays():
     rc = L.fvgb_rhs_noalloc(ctypes.byref(soa), ctypes.addressof(p), ctypes.addressof(dummy), ctypes.addressof(dummy),
                             None)
     assert rc == -1 and "NULL" in L.fvgb_last_error().decode()
+
+
+class _RoutineControllerStatement:
+    """The reference's adaptive CFL, restated from its rules (RoutineController.cpp:13-90)."""
+
+    def __init__(self):
+        self.calls, self.record = 0, 10.0
+        self.last = {"inc": 0, "dec": 0}
+        self.cold = {"inc": 1000, "dec": 500}
+
+    def _try(self, which, cfl, step, factor):
+        if step - self.last[which] >= self.cold[which]:
+            self.last[which] = step
+            return cfl * factor, True
+        return cfl, False
+
+    def apply(self, res, step, cfl):
+        ok = False
+        if self.calls == 0:
+            self.record = res
+        else:
+            if step > 1000 and res > self.record * 10.0:
+                cfl, a = self._try("dec", cfl, step, 0.75)
+                ok |= a
+            if step > 5000 and res < self.record * 0.5:
+                cfl, a = self._try("inc", cfl, step, 1.1)
+                if a:
+                    self.record *= 0.9
+                ok |= a
+            if step > 5000:
+                cfl, a = self._try("inc", cfl, step, 1.05)
+                ok |= a
+            cfl = max(cfl, 0.5)
+        self.calls += 1
+        return cfl, ok
+
+
+def test_adaptive_cfl_controller_follows_the_reference_rules():
+    L = fv.lib()
+    L.fvgb_cfl_controller_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    L.fvgb_cfl_controller_apply.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]
+    L.fvgb_cfl_controller_destroy.argtypes = [ctypes.c_void_p]
+    L.fvgb_cfl_controller_destroy.restype = None
+    rng = np.random.default_rng(4)
+    for trial in range(6):
+        c = ctypes.c_void_p()
+        assert L.fvgb_cfl_controller_create(1, ctypes.byref(c)) == 0
+        ref = _RoutineControllerStatement()
+        cfl = ctypes.c_double(0.8)
+        cfl_ref, changes = 0.8, 0
+        res = 1e-2
+        for step in [1] + list(range(50, 12001, 50)):
+            # residual histories that fall, jump up by orders of magnitude, and stall
+            res *= float(np.exp(rng.normal(-0.02, 0.3))) * (30.0 if rng.random() < 0.02 else 1.0)
+            applied = ctypes.c_int()
+            assert L.fvgb_cfl_controller_apply(c, res, step, ctypes.byref(cfl), ctypes.byref(applied)) == 0
+            cfl_ref, ok = ref.apply(res, step, cfl_ref)
+            assert cfl.value == cfl_ref and bool(applied.value) == ok, (trial, step)
+            changes += ok
+        assert changes > 3
+        L.fvgb_cfl_controller_destroy(c)
+    c = ctypes.c_void_p()
+    assert L.fvgb_cfl_controller_create(0, ctypes.byref(c)) == 0  # strategy 0 never changes CFL
+    cfl = ctypes.c_double(0.8)
+    for step in range(1, 20000, 97):
+        L.fvgb_cfl_controller_apply(c, 1e3 * step, step, ctypes.byref(cfl), None)
+    assert cfl.value == 0.8
+    L.fvgb_cfl_controller_destroy(c)
+    assert L.fvgb_cfl_controller_create(2, ctypes.byref(c)) == -1
+
+
+def test_time_strategy_key(tmp_path):
+    tp = tmp_path / "s.toml"
+    tp.write_text(cases.toml_text().replace("[time]\n", "[time]\nstrategy = 1\n"))
+    assert fv.run_config(str(tp))["time_strategy"] == 1
+    tp.write_text(cases.toml_text().replace("[time]\n", "[time]\nstrategy = 3\n"))
+    with pytest.raises(fv.FvgbError):
+        fv.run_config(str(tp))
