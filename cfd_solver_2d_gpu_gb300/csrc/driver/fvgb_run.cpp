@@ -35,6 +35,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -64,7 +65,7 @@ std::string step_tag(int istep) {
 }
 
 int usage() {
-    std::fprintf(stderr, "usage: fvgb_run input.toml [--output DIR] [--device N] [--quiet]\n");
+    std::fprintf(stderr, "usage: fvgb_run input.toml [--output DIR] [--device N] [--quiet] [--snapshot-seconds S]\n");
     return 1;
 }
 
@@ -76,10 +77,13 @@ int main(int argc, char** argv) {
     std::string out_dir = folder_of(toml) + "/output";
     int device = -1;
     bool quiet = false;
+    // a pause file every so many seconds of wall time (CDriver.h:33-34, 30 minutes)
+    double snapshot_seconds = 1800.0;
     for (int i = 2; i < argc; i++) {
         if (!std::strcmp(argv[i], "--output") && i + 1 < argc) out_dir = argv[++i];
         else if (!std::strcmp(argv[i], "--device") && i + 1 < argc) device = std::atoi(argv[++i]);
         else if (!std::strcmp(argv[i], "--quiet")) quiet = true;
+        else if (!std::strcmp(argv[i], "--snapshot-seconds") && i + 1 < argc) snapshot_seconds = std::atof(argv[++i]);
         else return usage();
     }
 
@@ -167,6 +171,8 @@ int main(int argc, char** argv) {
     std::string final_prefix = "pause_";
     auto next_multiple = [](int after, int every) { return (after / every + 1) * every; };
     int last_field_step = -1;
+    const auto t_start = std::chrono::steady_clock::now();
+    double last_snapshot = 0.0;
     while (istep < max_it) {
         // the next step at which CDriver::start would print or write (modifySignalPack1_output)
         int target = max_it;
@@ -214,6 +220,15 @@ int main(int argc, char** argv) {
         if (write_field) {
             if (write_fields(istep)) return 1;
             last_field_step = istep;
+        }
+        // modifySignalPack1_output's snapshot (CDriver.cpp:227-232): a pause file once the wall
+        // time since the last one exceeds the cool-down, checked here at each event
+        const double now = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        if (now - last_snapshot > snapshot_seconds) {
+            last_snapshot = now;
+            if (fvgb_get_state(h, U.data())) return report("fvgb_get_state");
+            const std::string snap = out_dir + "/pause_" + name + step_tag(istep) + ".dat";
+            if (fvgb_write_continue(mesh, snap.c_str(), t, istep, p.CFL, U.data())) return report(snap.c_str());
         }
         // modifySignalPack2_pause (CDriver.cpp:230-263)
         if (std::isnan(res[0])) {

@@ -121,3 +121,27 @@ def test_driver_adaptive_cfl(tmp_path):
     assert fv.lib().fvgb_set_cfl(s._h, ctypes.c_double(new)) == 0
     t2 = s.step(t1, p.T_end, 10)
     assert np.array_equal(s.get_state(), U) and t2 == t
+
+
+def test_driver_wall_time_snapshots(tmp_path):
+    """The reference writes a pause file whenever 30 minutes of wall time have passed since the
+    last one (CDriver.cpp:227-232); with the cool-down at 0 s every event writes one, each the
+    state of its step."""
+    d = str(tmp_path / "case")
+    tp = make_case(d, 20)
+    out = os.path.join(d, "out")
+    fv.lib()
+    r = subprocess.run([EXE, tp, "--output", out, "--snapshot-seconds", "0"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    pauses = sorted(f for f in os.listdir(out) if f.startswith("pause_"))
+    assert pauses == ["pause_jv[%04d].dat" % k for k in (1, 5, 10, 15, 20)], pauses
+    p = fv.Params.from_toml(tp)
+    m = fv.Mesh.read_su2(os.path.join(d, "jv.su2"), p)
+    s = fv.GPUSolver2(m, p)
+    t = s.step(0.0, p.T_end, 10)
+    _, U, t10, istep, _ = fv.Mesh.read_continue(os.path.join(out, "pause_jv[0010].dat"))
+    assert istep == 10 and t10 == t and np.array_equal(U, s.get_state())
+    d2 = str(tmp_path / "case2")
+    r = run(make_case(d2, 20), os.path.join(d2, "out"))  # the default cool-down: only the stop writes one
+    assert r.returncode == 0 and [f for f in os.listdir(os.path.join(d2, "out")) if f.startswith("pause_")] == \
+        ["pause_jv[0020].dat"]
