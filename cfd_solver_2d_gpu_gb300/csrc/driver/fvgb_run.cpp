@@ -36,6 +36,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <csignal>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -47,6 +48,11 @@
 #include "fvgb.h"
 
 namespace {
+
+// SIGINT / SIGTERM play the reference's ESC key (CDriver.cpp:244-249): the run stops at its
+// next event and writes its pause file
+volatile std::sig_atomic_t g_stop = 0;
+void on_signal(int) { g_stop = 1; }
 
 int report(const char* what) {
     std::fprintf(stderr, "fvgb_run: %s: %s\n", what, fvgb_last_error());
@@ -172,6 +178,8 @@ int main(int argc, char** argv) {
     auto next_multiple = [](int after, int every) { return (after / every + 1) * every; };
     int last_field_step = -1;
     const auto t_start = std::chrono::steady_clock::now();
+    std::signal(SIGINT, on_signal);
+    std::signal(SIGTERM, on_signal);
     double last_snapshot = 0.0;
     while (istep < max_it) {
         // the next step at which CDriver::start would print or write (modifySignalPack1_output)
@@ -235,6 +243,10 @@ int main(int argc, char** argv) {
             status = 2;
             why = "NaN detected";
             final_prefix = "nan_";
+            break;
+        }
+        if (g_stop) {
+            why = "stopped by a signal";
             break;
         }
         if (t >= T) {

@@ -145,3 +145,33 @@ def test_driver_wall_time_snapshots(tmp_path):
     r = run(make_case(d2, 20), os.path.join(d2, "out"))  # the default cool-down: only the stop writes one
     assert r.returncode == 0 and [f for f in os.listdir(os.path.join(d2, "out")) if f.startswith("pause_")] == \
         ["pause_jv[0020].dat"]
+
+
+def test_driver_stops_on_a_signal(tmp_path):
+    """SIGINT plays the reference's ESC key (CDriver.cpp:244-249): the run stops at its next
+    event and writes the pause file of that step."""
+    import signal
+    d = str(tmp_path / "case")
+    tp = make_case(d, 10_000_000)
+    out = os.path.join(d, "out")
+    fv.lib()
+    proc = subprocess.Popen([EXE, tp, "--output", out], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    try:
+        for line in proc.stdout:
+            if line.startswith("step = 200\t"):
+                proc.send_signal(signal.SIGINT)
+                break
+        rest, err = proc.communicate(timeout=60)
+    finally:
+        if proc.poll() is None:
+            proc.kill()
+            proc.wait()
+    assert proc.returncode == 0, err
+    pauses = [f for f in os.listdir(out) if f.startswith("pause_")]
+    assert len(pauses) == 1
+    _, U, t, istep, _ = fv.Mesh.read_continue(os.path.join(out, pauses[0]))
+    assert 200 <= istep < 10_000_000 and "stopped by a signal" in rest
+    p = fv.Params.from_toml(tp)
+    s = fv.GPUSolver2(fv.Mesh.read_su2(os.path.join(d, "jv.su2"), p), p)
+    t2 = s.step(0.0, p.T_end, istep)
+    assert np.array_equal(s.get_state(), U) and t2 == t
