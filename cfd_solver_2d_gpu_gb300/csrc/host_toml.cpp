@@ -333,6 +333,11 @@ extern "C" int fvgb_params_read_toml(const char* path, fvgb_params* p, char* mes
     }
     r.integer("output.maxIteration", p->max_iteration, false);
     r.integer("physicsModel.equation", p->equation, true);
+    {  // CInput::readConfig accepts only 2D (CInput.cpp:55)
+        int dim = 2;
+        r.integer("basic.dimension", dim, false);
+        if (dim != 2) return fail(FVGB_ERR_FORMAT, "input.toml: basic.dimension must be 2");
+    }
     bool steady = false;
     r.boolean("time.is_steady", steady, false);
     p->steady = steady ? 1 : 0;

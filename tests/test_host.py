@@ -299,3 +299,11 @@ def test_time_strategy_key(tmp_path):
     tp.write_text(cases.toml_text().replace("[time]\n", "[time]\nstrategy = 3\n"))
     with pytest.raises(fv.FvgbError):
         fv.run_config(str(tp))
+
+
+def test_dimension_other_than_2_is_refused(tmp_path):
+    tp = tmp_path / "d.toml"
+    tp.write_text(cases.toml_text().replace("dimension = 2", "dimension = 3"))
+    with pytest.raises(fv.FvgbError) as e:
+        fv.Params.from_toml(str(tp))
+    assert "dimension" in str(e.value)
