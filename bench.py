@@ -13,6 +13,7 @@ cell-stage updates per second = cells x 3 x steps / time.  Every array of the
 step is larger than the 129 MB L2, so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--flux roe|llf]
+                    [--workload vortex_large|cylinder_ns|batch|adjoint|output]
 
 Multi-GPU: the path is single-GPU; with N > 1 every rank runs an independent
 replica of the workload (weak scaling, no collective on the data path) and the
@@ -46,8 +47,10 @@ def parse():
     ap.add_argument("--n", type=int, default=N_SIDE, help="cells per side of the square (default 1448)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=["vortex_large", "batch", "adjoint", "output"], default="vortex_large",
-                    help="batch: many cylinder instances in one persistent launch per stage vs the same "
+    ap.add_argument("--workload", choices=["vortex_large", "cylinder_ns", "batch", "adjoint", "output"],
+                    default="vortex_large",
+                    help="cylinder_ns: the laminar cylinder O-grid (512 x 256 quads, Navier-Stokes, Kutta RK3) "
+                         "through the plain path; batch: many cylinder instances in one persistent launch per stage vs the same "
                          "instances stepped one after another through the plain path; adjoint: the discrete "
                          "adjoint through K SSP-RK3 steps on the 256x256 jittered vortex")
     ap.add_argument("--batch-n", type=int, default=256)
@@ -276,11 +279,22 @@ def dist_env():
 def workload(args, directory):
     from cfd_solver_2d_gpu_gb300 import cases
     flux = 2002 if args.flux == "roe" else 2001
-    tp, su2 = cases.vortex_large(directory, n=args.n, flux=flux)
+    if args.workload == "cylinder_ns":  # the laminar cylinder O-grid, 512 x 256 quads
+        tp, su2 = cases.cylinder_ns(directory, flux=flux)
+    else:
+        tp, su2 = cases.vortex_large(directory, n=args.n, flux=flux)
     return tp, su2, flux
 
 
 def config(args, N, E, V):
+    if args.workload == "cylinder_ns":
+        return {"workload": f"laminar cylinder O-grid 512x256 quads -> {N} triangles, Navier-Stokes, Ma 0.2, Re 100, "
+                            f"second order (LSQ + Barth), {args.flux.upper()} flux, Kutta RK3, CFL 0.5",
+                "cells": N, "edges": E, "nodes": V, "stages_per_step": 3,
+                "gradient": "least squares (reference determinant guard) + Barth", "flux": args.flux,
+                "integrator": "Kutta RK3", "l2_flush": "none: the per-step arrays (about 0.2 GB) exceed the L2 only "
+                                                       "together",
+                "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
     return {"workload": f"jittered periodic vortex {args.n}x{args.n} quads -> {N} triangles, second order "
                         f"(LSQ + Barth), {args.flux.upper()} flux, SSP-RK3, CFL 0.8",
             "cells": N, "edges": E, "nodes": V, "stages_per_step": 3,
@@ -500,7 +514,8 @@ def main():
         avg_ms = prof[dom][0] / prof[dom][1]
         peak, peak_kind = measured_peaks()
         achieved = algo[dom] / (avg_ms / 1e3) / 1e9
-        ncu = ncu_figures(args.flux, N)
+        # the committed per-launch ncu figures are of the vortex workload's kernels
+        ncu = ncu_figures(args.flux, N) if args.workload == "vortex_large" else {}
         traffic = ncu.get(dom, {}).get("dram_bytes_per_launch")
         stage_ms = (prof["gradient"][0] + prof["flux"][0] + prof["update"][0]) / max(prof["update"][1], 1)
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
