@@ -4,8 +4,8 @@
   initial field, with an error that falls at second order as the mesh is refined
   in the corrected least-squares mode ([gpu] lsq_det = "fixed"); in the
   reference's own mode (MatrixKernel.h:48-49 turns every determinant above 1e-10
-  into -1e-10) the gradients are unusable, the reconstruction falls back to the
-  cell values, and the error stalls, which the test records as well;
+  into -1e-10, scaling the gradients by -det/1e-10) the limiter keeps the face
+  values bounded but the order stays below one, which the test records as well;
 - the Sod shock tube on the quasi-one-dimensional channel follows the exact
   solution of the Riemann problem (Toro's exact solver, Riemann Solvers and
   Numerical Methods for Fluid Dynamics, ch. 4: Newton iteration on the pressure
