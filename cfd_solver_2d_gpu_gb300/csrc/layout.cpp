@@ -35,12 +35,15 @@ uint64_t spread(uint32_t x) {
 }
 bool is_periodic(int t) { return t >= BC_PERIODIC_0 && t <= BC_PERIODIC_9; }
 
+}  // namespace
+
 // The caller's arrays are checked before anything indexes them, so that a bad
 // index is an error code rather than a host crash or an out-of-bounds gather on
 // the device (every device index is derived from these).
 int validate_mesh(const fvgb_mesh_soa& m) {
     const int N = m.num_element, E = m.num_edge, V = m.num_node, NB = m.num_boundary;
     if (N < 0 || E < 0 || V < 0 || NB < 0) return fail(FVGB_ERR_MESH, "negative mesh sizes");
+    if (N == 0) return fail(FVGB_ERR_MESH, "mesh has no cells");  // as the su2 reader refuses one
     if ((N > 0 && (!m.elem_edges || !m.elem_nodes || !m.elem_neighbors || !m.elem_xy || !m.elem_volume)) ||
         (E > 0 && (!m.edge_L || !m.edge_R || !m.edge_setID || !m.edge_periodicPair || !m.edge_length ||
                    !m.edge_xy || !m.edge_normal || !m.edge_nodes)) ||
@@ -68,7 +71,6 @@ int validate_mesh(const fvgb_mesh_soa& m) {
     }
     return 0;
 }
-}  // namespace
 
 int build_layout(const fvgb_mesh_soa& m, const fvgb_params& p, Layout& L) {
     if (int rc = validate_mesh(m)) return rc;

@@ -28,6 +28,9 @@ struct Layout {
     std::vector<int> dt_ptr, dt_edge;  // CSR: edges whose spectral radius a cell sums
 };
 
+// Checks the caller's mesh arrays (sizes, NULL arrays, every index in range) on the
+// host; FVGB_ERR_MESH with the reason, 0 if the mesh may be indexed.
+int validate_mesh(const fvgb_mesh_soa& m);
 int build_layout(const fvgb_mesh_soa& m, const fvgb_params& p, Layout& L);
 
 }  // namespace fvgb

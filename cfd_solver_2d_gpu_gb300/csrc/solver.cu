@@ -109,6 +109,7 @@ int Solver::init(const fvgb_mesh_soa& m, const fvgb_params& prm) {
     p = prm;
     int rc = check_params(p);
     if (rc) return rc;
+    if ((rc = validate_mesh(m))) return rc;  // host-only checks first: a bad mesh is refused without a device
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(FVGB_ERR_NO_DEVICE, "no CUDA device");
     if (p.device < 0 || p.device >= ndev) return fail(FVGB_ERR_ARG, "device ordinal out of range");

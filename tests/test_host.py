@@ -205,6 +205,54 @@ def test_steady_inputs(tmp_path):
     assert "is_steady" in str(e.value)
 
 
+def test_create_refuses_bad_meshes_on_the_host(tmp_path):
+    """fvgb_create checks the caller's mesh before it looks for a device: an empty mesh,
+    a NULL array and an index outside the mesh are FVGB_ERR_MESH (-4) here, without a
+    GPU; a good mesh gets as far as the device check (-10 without a GPU)."""
+    L = fv.lib()
+    tp, su2 = cases.vortex_small(str(tmp_path), n=6)
+    p = fv.Params.from_toml(tp)
+    m = fv.Mesh.read_su2(su2, p)
+
+    def create(soa):
+        h = ctypes.c_void_p()
+        rc = L.fvgb_create(ctypes.byref(soa), ctypes.byref(p), ctypes.byref(h))
+        if rc == 0:
+            L.fvgb_destroy(h)
+        return rc, L.fvgb_last_error().decode()
+
+    def copy():
+        soa = fv.MeshSoA()
+        ctypes.memmove(ctypes.byref(soa), ctypes.byref(m.soa), ctypes.sizeof(soa))
+        return soa
+
+    empty = fv.MeshSoA()
+    assert create(empty) == (-4, "mesh has no cells")
+    soa = copy()
+    soa.edge_normal = None
+    assert create(soa) == (-4, "a mesh array is NULL")
+    keep = []
+    for name, index, value in (("edge_L", 3, m.N), ("edge_R", 0, -2), ("edge_setID", m.E - 1, m.NB + 1),
+                               ("elem_edges", 5, m.E), ("elem_neighbors", 2, m.N)):
+        arr = np.ascontiguousarray(m.array(name)).copy()
+        arr.reshape(-1)[index] = value
+        keep.append(arr)
+        soa = copy()
+        setattr(soa, name, arr.ctypes.data)
+        rc, msg = create(soa)
+        assert rc == -4 and "outside" in msg, (name, rc, msg)
+    if not torch_cuda_available():
+        assert create(copy())[0] == -10
+
+
+def torch_cuda_available():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except ImportError:
+        return False
+
+
 def test_rhs_noalloc_refuses_null_mesh_arrays():
     """fvgb_rhs_noalloc reads the caller's device arrays; a NULL among them is refused on the
     host before anything is launched (no GPU needed to see it)."""
