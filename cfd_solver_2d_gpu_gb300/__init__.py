@@ -107,6 +107,7 @@ def lib():
             "fvgb_time": (i, [v, dp, dp]),
             "fvgb_synchronize": (i, [v]),
             "fvgb_rhs": (i, [v, dp, dp, dp, dp]),
+            "fvgb_rhs_vjp": (i, [v, dp, dp, dp]),
             "fvgb_dt": (i, [v, dp]),
             "fvgb_residual": (i, [v, i, dp]),
             "fvgb_device_status": (i, [v, ctypes.POINTER(ctypes.c_longlong)]),
@@ -347,6 +348,14 @@ class GPUSolver2:
         gy = np.empty_like(U) if gradients else None
         _check(lib().fvgb_rhs(self._h, _dp(U), _dp(R), _dp(gx), _dp(gy)))
         return (R, gx, gy) if gradients else R
+
+    def rhs_vjp(self, U, seed):
+        """(dR/dU)^T seed at U, R = rhs(U) (fvgb_rhs_vjp); arrays [4][N], reference numbering."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        seed = np.ascontiguousarray(seed, dtype=np.float64)
+        g = np.empty_like(U)
+        _check(lib().fvgb_rhs_vjp(self._h, _dp(U), _dp(seed), _dp(g)))
+        return g
 
     def dt(self):
         out = ctypes.c_double()

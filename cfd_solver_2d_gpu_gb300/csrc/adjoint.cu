@@ -493,6 +493,7 @@ struct Adjoint {
     d4 *d_lamdir = nullptr, *d_bdU = nullptr, *d_keepU = nullptr;
     int *d_rlist = nullptr, *d_rev = nullptr;
     double* d_dotp = nullptr;
+    double* d_one = nullptr;  // 1.0: the time step of rhs_vjp's reverse
     bool ready = false;
     bool last_kept = false;  // the segment buffers hold the last segment's steps
     long long restricted_before = 0;
@@ -509,11 +510,13 @@ struct Adjoint {
         return 0;
     }
 
-    int setup(Solver* solver, int nsteps, int ncheck) {
+    // rhs_only: the workspace of one recorded residual (rhs_vjp), whatever the time scheme
+    int setup(Solver* solver, int nsteps, int ncheck, bool rhs_only = false) {
         s = solver;
         const fvgb_params& p = s->p;
         if (p.equation != 1 && p.equation != 2) return fail(FVGB_ERR_ARG, "invalid equation");
-        if (p.steady) return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers time-accurate runs (time.is_steady = 0)");
+        if (p.steady && !rhs_only)
+            return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers time-accurate runs (time.is_steady = 0)");
         if (p.flux_scheme != 2001 && p.flux_scheme != 2002) return fail(FVGB_ERR_ARG, "invalid flux scheme");
         if (p.time_advance != 3101 && p.time_advance != 3103 && p.time_advance != 3104)
             return fail(FVGB_ERR_ARG, "invalid time_advance");
@@ -526,7 +529,7 @@ struct Adjoint {
         ncheck = std::max(1, std::min(ncheck, K));
         S = (K + ncheck - 1) / ncheck;
         nseg = (K + S - 1) / S;
-        nst = p.time_advance == 3101 ? 1 : 3;
+        nst = (rhs_only || p.time_advance == 3101) ? 1 : 3;
         const int N = s->N, E = s->E;
         // R-list flag per edge (interior non-periodic edges appear in R's edge list)
         std::vector<int> rlist(E, 0);
@@ -580,9 +583,12 @@ struct Adjoint {
             (rc = alloc(d_lamdir, N)) || (rc = alloc(d_keepU, N)) || (rc = alloc(d_bdU, 3 * (size_t)N)) ||
             (rc = alloc(d_dotp, (size_t)nb * 3)))
             return rc;
-        if (p.time_advance == 3103 &&
+        if (p.time_advance == 3103 && !rhs_only &&
             ((rc = alloc(d_k_a2, N)) || (rc = alloc(d_k_a1, N)) || (rc = alloc(d_k_seed, N))))
             return rc;
+        if ((rc = alloc(d_one, 1))) return rc;
+        static const double kOne = 1.0;
+        AK(cudaMemcpyAsync(d_one, &kOne, sizeof(double), cudaMemcpyHostToDevice, s->stream));
         if (p.reconstruct == 3002 && p.gradient == 2) {
             // ggrev[c][k]: the face of cell q = ggout[c][k] whose far cell is c; where c and q
             // share several faces (tiny periodic meshes), the m-th such face of c is paired with
@@ -789,6 +795,45 @@ struct Adjoint {
         return 0;
     }
 
+    // (dR/dU)^T seed at U, R = fvgb_rhs(U): one recorded evaluation of R made as
+    // Solver::rhs makes it ("dsr" edges at the handle's time), then the stage reverse
+    // with dt = 1 and no identity term (b = 1, ci = 0: lam_in = J^T seed exactly)
+    int rhs_vjp(const double* U, const double* seed, double* grad) {
+        Solver& v = *s;
+        cudaStream_t st = v.stream;
+        int rc;
+        if ((rc = v.set_state(U))) return rc;
+        const bool ns = v.p.equation == 2;
+        const dev::CellTape ct = seg_ctape.empty() ? dev::CellTape() : seg_ctape[0];
+        if (v.needs_gradient()) {
+            dev::launch_grad(st, v.p.gradient, v.p.limiter == 1, v.d_U, v.mv, v.d_Gx, v.d_Gy, ct.gx ? &ct : nullptr);
+            v.launches += 1;
+        }
+        dev::BcData b = v.bc;
+        b.clock_t0 = &v.d_state->t;
+        b.clock_dt = &v.d_state->dt;
+        b.clock_frac = 0.0;
+        dev::EdgeTape tp;
+        tp.v = seg_tape[0];
+        tp.flags = seg_tflags[0];
+        tp.E = v.E;
+        dev::launch_flux(st, v.p.flux_scheme, v.p.reconstruct == 3002, ns, v.d_U, v.d_Gx, v.d_Gy, v.mv, v.gas, b,
+                         v.d_F, v.d_status, &tp);
+        dev::launch_update(st, dev::STAGE_RHS, v.d_U, v.d_U0, v.d_K1, seg_R[0], v.d_F, v.mv, v.d_state, v.gas,
+                           v.d_flags, v.d_flag_count, Solver::kFlagCap, v.d_status);
+        v.launches += 1 + (v.mv.E_int > 0) + (v.mv.E > v.mv.E_int);
+        AK(cudaMemcpyAsync(v.d_stage, seed, sizeof(double) * 4 * v.N, cudaMemcpyHostToDevice, st));
+        dev::launch_scatter_in(st, v.d_stage, d_lam, v.d_cell_new, v.N);
+        vis_gx = ns ? v.d_Gx : nullptr;  // the viscous reverse reads the gradients of this evaluation
+        vis_gy = ns ? v.d_Gy : nullptr;
+        if ((rc = stage_vjp(v.d_U, tp, ct, seg_R[0], d_one, 0.0, 1.0, 2, 0, d_lam, d_lam_in, 0.0))) return rc;
+        v.launches += 4;
+        dev::launch_gather_out(st, d_lam_in, v.d_stage, v.d_cell_new, v.N);
+        AK(cudaMemcpyAsync(grad, v.d_stage, sizeof(double) * 4 * v.N, cudaMemcpyDeviceToHost, st));
+        AK(cudaStreamSynchronize(st));
+        return v.check_status();
+    }
+
     // the state and time at the start of segment i
     int load_segment(int i) {
         Solver& v = *s;
@@ -903,11 +948,18 @@ struct AdjHandle {
     fvgb_handle* owner;
     Adjoint adj;
 };
-std::vector<AdjHandle*> g_adj;  // one adjoint workspace per handle (handles are single-threaded)
-AdjHandle* find_adj(fvgb_handle* h) {
-    for (auto* a : g_adj)
+std::vector<AdjHandle*> g_adj;      // one adjoint workspace per handle (handles are single-threaded)
+std::vector<AdjHandle*> g_adj_rhs;  // and one for fvgb_rhs_vjp, kept between calls
+AdjHandle* find_adj(fvgb_handle* h, std::vector<AdjHandle*>& reg = g_adj) {
+    for (auto* a : reg)
         if (a->owner == h) return a;
     return nullptr;
+}
+void drop_adj(fvgb_handle* h, std::vector<AdjHandle*>& reg) {
+    if (AdjHandle* a = find_adj(h, reg)) {
+        reg.erase(std::find(reg.begin(), reg.end(), a));
+        delete a;
+    }
 }
 }  // namespace
 
@@ -943,9 +995,22 @@ extern "C" int fvgb_adjoint_backward(fvgb_handle* h, const double* seed_UK, doub
 }
 
 extern "C" void fvgb_adjoint_release(fvgb_handle* h) {
-    AdjHandle* a = find_adj(h);
-    if (a) {
-        g_adj.erase(std::find(g_adj.begin(), g_adj.end(), a));
-        delete a;
+    drop_adj(h, g_adj);
+    drop_adj(h, g_adj_rhs);
+}
+
+// No counterpart in the reference: see include/fvgb.h.
+extern "C" int fvgb_rhs_vjp(fvgb_handle* h, const double* U, const double* seed_R, double* grad_U) {
+    if (!h || !U || !seed_R || !grad_U) return fail(FVGB_ERR_ARG, "null argument");
+    cudaSetDevice(h->s.p.device);
+    AdjHandle* a = find_adj(h, g_adj_rhs);
+    if (!a) {
+        a = new AdjHandle{h, Adjoint()};
+        if (int rc = a->adj.setup(&h->s, 1, 1, true)) {
+            delete a;
+            return rc;
+        }
+        g_adj_rhs.push_back(a);
     }
+    return a->adj.rhs_vjp(U, seed_R, grad_U);
 }

@@ -285,6 +285,16 @@ int fvgb_adjoint_forward(fvgb_handle* h, int nsteps, int n_checkpoints, const do
                          double* ms_forward);
 int fvgb_adjoint_backward(fvgb_handle* h, const double* seed_UK, double* grad_U0, double* ms_backward);
 void fvgb_adjoint_release(fvgb_handle* h);
+/* The residual's vector-Jacobian product grad_U = (dR/dU)^T seed_R at the state U,
+ * where R is what fvgb_rhs returns for U (calculateFunctionF, FVMR/src/time/
+ * Evolve.cpp:98-112): the reverse of the edge fluxes with their boundary ghosts,
+ * the face reconstruction, the Barth limiter and the gradients, in the scope of
+ * the adjoint above (steady runs included: R does not involve the time step).
+ * These are the reverse kernels of one Runge-Kutta stage of fvgb_adjoint_backward,
+ * run once on a recorded evaluation of R.  U, seed_R, grad_U: [4][N], reference
+ * numbering; the handle's state becomes U, as with fvgb_rhs.  No counterpart in
+ * the reference. */
+int fvgb_rhs_vjp(fvgb_handle* h, const double* U, const double* seed_R, double* grad_U);
 
 /* ---- batched instances -----------------------------------------------------
  * No counterpart in the reference (one mesh per process, the driver loop of

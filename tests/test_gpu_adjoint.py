@@ -262,3 +262,41 @@ def test_adjoint_navier_stokes(tmp_path, kind):
     errs, g = fd_check(solver, p, U0, rho_t, K, 6)
     assert np.all(np.isfinite(g))
     assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+
+
+@pytest.mark.parametrize("kind", ["vortex_lsq_barth_roe", "vortex_gg_llf", "vortex_o1", "channel_subsonic",
+                                  "vortex_ns", "channel_ns_gg", "vortex_steady"])
+def test_rhs_vjp_matches_fd(tmp_path, kind):
+    """fvgb_rhs_vjp, (dR/dU)^T seed, against central finite differences of fvgb_rhs
+    (seed . (R(U + h d) - R(U - h d)) / 2h against d . grad, random unit directions d)."""
+    d = str(tmp_path)
+    channel = dict(vortex=(2.5, 7.0, 3.0), inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0),
+                   outlet=(1.0, 1.0, 0.0, 0.9))
+    if kind.startswith("vortex"):
+        su2 = cases.square_mesh(16, jitter=0.2, directory=d)
+    else:
+        su2 = cases.channel_mesh(12, jitter=0.2, directory=d)
+    cfg = {"vortex_lsq_barth_roe": dict(flux=2002, reconstruct=3002, gradient=1, limiter=1),
+           "vortex_gg_llf": dict(flux=2001, reconstruct=3002, gradient=2, limiter=1),
+           "vortex_o1": dict(flux=2002, reconstruct=3001, gradient=1, limiter=1),
+           "channel_subsonic": dict(flux=2002, reconstruct=3002, gradient=1, limiter=1, **channel),
+           "vortex_ns": dict(equation=2, flux=2002, reconstruct=3002, gradient=1, limiter=1, Re=100.0),
+           "channel_ns_gg": dict(equation=2, flux=2002, reconstruct=3002, gradient=2, limiter=1, Re=100.0, **channel),
+           "vortex_steady": dict(flux=2002, reconstruct=3002, gradient=1, limiter=1, steady=1)}[kind]
+    text = cases.toml_text(time_advance=3104, CFL=0.6, **cfg)
+    p, solver, U0, _ = boundary_case(tmp_path, kind, text, su2)
+    rng = np.random.default_rng(5)
+    lam = rng.standard_normal(U0.shape)
+    g = solver.rhs_vjp(U0, lam)
+    assert np.all(np.isfinite(g))
+    assert np.array_equal(solver.get_state(), U0)  # the handle's state is U, as after rhs
+    assert np.array_equal(solver.rhs_vjp(U0, lam), g)  # the cached workspace: same bits again
+    errs = []
+    for _ in range(6):
+        dU = rng.standard_normal(U0.shape)
+        dU /= np.linalg.norm(dU)
+        fd = float(np.sum(lam * (solver.rhs(U0 + H * dU) - solver.rhs(U0 - H * dU)))) / (2 * H)
+        ad = float(np.sum(g * dU))
+        errs.append(abs(fd - ad) / max(abs(fd), 1e-30))
+    errs = np.array(errs)
+    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
