@@ -152,6 +152,22 @@ def test_torch_autograd_function(tmp_path):
     assert np.allclose(x.grad.numpy(), g, rtol=0, atol=1e-14 * np.abs(g).max())
 
 
+def test_torch_autograd_rhs(tmp_path):
+    """The residual's wrapper: torch's backward through R(U) is fvgb_rhs_vjp, and the
+    directional derivative it gives matches a central difference of R."""
+    torch = pytest.importorskip("torch")
+    from cfd_solver_2d_gpu_gb300.autograd import rhs
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=12)
+    w = torch.from_numpy(np.random.default_rng(2).standard_normal(U0.shape))
+    x = torch.from_numpy(U0.copy()).requires_grad_(True)
+    (rhs(x, solver) * w).sum().backward()
+    assert np.array_equal(x.grad.numpy(), solver.rhs_vjp(U0, w.numpy()))
+    d = np.random.default_rng(3).standard_normal(U0.shape)
+    d /= np.linalg.norm(d)
+    fd = float(np.sum(w.numpy() * (solver.rhs(U0 + H * d) - solver.rhs(U0 - H * d)))) / (2 * H)
+    assert abs(fd - float(np.sum(x.grad.numpy() * d))) <= 1e-6 * abs(fd)
+
+
 def test_adjoint_matches_fd_kutta_rk3(tmp_path):
     """Kutta RK3 (3103): the stages' seeds s3 = L3/6, s2 = 2/3 L3 + 2 L2, s1 = L3/6 - L2 + L1/2."""
     tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=16, time_advance=3103, CFL=0.6)
