@@ -32,6 +32,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -948,18 +949,34 @@ struct AdjHandle {
     fvgb_handle* owner;
     Adjoint adj;
 };
-std::vector<AdjHandle*> g_adj;      // one adjoint workspace per handle (handles are single-threaded)
-std::vector<AdjHandle*> g_adj_rhs;  // and one for fvgb_rhs_vjp, kept between calls
+// One adjoint workspace per handle, and one for fvgb_rhs_vjp kept between calls.  A handle is
+// used by one thread at a time, but different handles may be used from different threads, so
+// the registries themselves are guarded; the work on a workspace runs outside the lock.
+std::mutex g_adj_mu;
+std::vector<AdjHandle*> g_adj;
+std::vector<AdjHandle*> g_adj_rhs;
 AdjHandle* find_adj(fvgb_handle* h, std::vector<AdjHandle*>& reg = g_adj) {
+    std::lock_guard<std::mutex> lk(g_adj_mu);
     for (auto* a : reg)
         if (a->owner == h) return a;
     return nullptr;
 }
+void add_adj(AdjHandle* a, std::vector<AdjHandle*>& reg) {
+    std::lock_guard<std::mutex> lk(g_adj_mu);
+    reg.push_back(a);
+}
 void drop_adj(fvgb_handle* h, std::vector<AdjHandle*>& reg) {
-    if (AdjHandle* a = find_adj(h, reg)) {
-        reg.erase(std::find(reg.begin(), reg.end(), a));
-        delete a;
+    AdjHandle* a = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_adj_mu);
+        for (auto it = reg.begin(); it != reg.end(); ++it)
+            if ((*it)->owner == h) {
+                a = *it;
+                reg.erase(it);
+                break;
+            }
     }
+    delete a;
 }
 }  // namespace
 
@@ -967,19 +984,15 @@ extern "C" int fvgb_adjoint_forward(fvgb_handle* h, int nsteps, int n_checkpoint
                                     double* U_K, double* ms_forward) {
     if (!h || !U0 || nsteps <= 0) return fail(FVGB_ERR_ARG, "bad adjoint arguments");
     cudaSetDevice(h->s.p.device);
-    AdjHandle* a = find_adj(h);
-    if (a) {
-        g_adj.erase(std::find(g_adj.begin(), g_adj.end(), a));
-        delete a;
-    }
-    a = new AdjHandle{h, Adjoint()};
+    drop_adj(h, g_adj);
+    AdjHandle* a = new AdjHandle{h, Adjoint()};
     int rc = a->adj.setup(&h->s, nsteps, n_checkpoints);
     if (!rc) rc = a->adj.forward(U0, t0, U_K);
     if (rc) {
         delete a;
         return rc;
     }
-    g_adj.push_back(a);
+    add_adj(a, g_adj);
     if (ms_forward) *ms_forward = a->adj.ms_fwd;
     return 0;
 }
@@ -1010,7 +1023,7 @@ extern "C" int fvgb_rhs_vjp(fvgb_handle* h, const double* U, const double* seed_
             delete a;
             return rc;
         }
-        g_adj_rhs.push_back(a);
+        add_adj(a, g_adj_rhs);
     }
     return a->adj.rhs_vjp(U, seed_R, grad_U);
 }

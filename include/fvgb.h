@@ -9,7 +9,9 @@
  *   - host arrays are in the reference's numbering and its [var][index] SoA
  *     layout (U[4][N] is 4 rows of N doubles);
  *   - one handle = one GPU, one CUDA stream, all device memory owned by the
- *     handle; a handle is used from one host thread at a time.
+ *     handle; a handle is used from one host thread at a time, and different
+ *     handles may be used from different threads at once (the error message
+ *     of fvgb_last_error is per thread).
  */
 #ifndef FVGB_H
 #define FVGB_H

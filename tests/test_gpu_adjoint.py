@@ -316,3 +316,35 @@ def test_rhs_vjp_matches_fd(tmp_path, kind):
         errs.append(abs(fd - ad) / max(abs(fd), 1e-30))
     errs = np.array(errs)
     assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+
+
+def test_handles_in_parallel_threads(tmp_path):
+    """Two handles driven from two host threads at once (ctypes releases the GIL during
+    each call): the adjoint's and the residual VJP's per-handle workspaces are registered
+    concurrently, and each thread's results equal the same calls made one after another."""
+    import threading
+    tp, su2, p, mesh, a, U0, Ut0 = setup_case(tmp_path, n=16)
+    b = fv.GPUSolver2(mesh, p)
+    lam = np.random.default_rng(4).standard_normal(U0.shape)
+    seed = np.random.default_rng(6).standard_normal(U0.shape)
+
+    def work_a(out):
+        for _ in range(3):
+            UK, _ = adjoint_forward(a, U0, 5, 2)
+            out.append(adjoint_backward(a, seed)[0])
+            fv.lib().fvgb_adjoint_release(a._h)
+
+    def work_b(out):
+        for _ in range(6):
+            out.append(b.rhs_vjp(U0, lam))
+            fv.lib().fvgb_adjoint_release(b._h)
+
+    ra, rb = [], []
+    ta, tb = threading.Thread(target=work_a, args=(ra,)), threading.Thread(target=work_b, args=(rb,))
+    ta.start(); tb.start(); ta.join(); tb.join()
+    adjoint_forward(a, U0, 5, 2)
+    ga = adjoint_backward(a, seed)[0]
+    gb = b.rhs_vjp(U0, lam)
+    assert len(ra) == 3 and len(rb) == 6
+    assert all(np.array_equal(g, ga) for g in ra)
+    assert all(np.array_equal(g, gb) for g in rb)
