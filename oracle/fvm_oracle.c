@@ -1202,7 +1202,7 @@ int om_run(const om_mesh* m, const om_params* p, double* U, int nsteps, double* 
     return rc;
 }
 
-/* get_residual_host, FVMR/src/output/residual/Residual.cpp:4-43 */
+/* host threads of the oracle's loops (n <= 0 leaves the count as it is); returns the count */
 int om_set_threads(int n) {
 #ifdef _OPENMP
     if (n > 0) omp_set_num_threads(n);
@@ -1213,6 +1213,7 @@ int om_set_threads(int n) {
 #endif
 }
 
+/* get_residual_host, FVMR/src/output/residual/Residual.cpp:4-43 */
 void om_residual(const om_mesh* m, const double* rhs, int norm, double* out) {
     const int N = m->N;
     for (int v = 0; v < 4; v++) {

@@ -80,7 +80,7 @@ def lib():
 
 
 def set_threads(n):
-    """Host threads of the oracle's loops; returns the count in use."""
+    """Host threads of the oracle's loops (n <= 0 only reads them); returns the count in use."""
     return lib().om_set_threads(int(n))
 
 

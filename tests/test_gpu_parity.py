@@ -213,6 +213,29 @@ def test_nan_is_an_error_code_not_a_crash():
     s.step(0.0, p.T_end, 1)
 
 
+def test_full_size_step_matches_the_oracle(tmp_path):
+    """The bench workload itself, 1448x1448 jittered vortex (4,193,408 cells), LSQ + Barth,
+    Roe, SSP-RK3, CFL 0.8: the residual and one step against the oracle on the same
+    inputs (the oracle's loops on all host threads, a few seconds)."""
+    import os
+    from oracle import pyoracle
+    tp, su2 = cases.vortex_large(str(tmp_path))
+    before = pyoracle.set_threads(0)  # 0 only reads the count
+    pyoracle.set_threads(os.cpu_count() or 1)
+    try:
+        o = Oracle(tp, su2)
+        s, p, m = make(tp, su2)
+        U0 = o.init_field()
+        assert rel(s.rhs(U0), o.rhs(U0)[0]) <= 1e-12
+        U, t, _, _ = o.run(U0, 1)
+    finally:
+        pyoracle.set_threads(before)
+    s.set_state(U0)
+    tg = s.step(0.0, p.T_end, 1)
+    assert abs(tg - t) <= 1e-12 * t
+    assert rel(s.get_state(), U) <= 1e-12
+
+
 def test_large_mesh_properties(tmp_path):
     """1448x1448 jittered vortex (4,193,408 cells), second order, SSP-RK3: total mass
     and energy are conserved on the periodic domain and the residual is finite."""
