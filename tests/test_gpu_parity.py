@@ -173,13 +173,23 @@ def test_second_order_200_steps(tmp_path, flux):
     assert err_g < 1e-2
 
 
-def test_against_oracle_cylinder_ns(tmp_path):
-    tp, su2 = cases.cylinder_ns(str(tmp_path), 128, 64)
+@pytest.mark.parametrize("size", [(128, 64), (512, 256)])
+def test_against_oracle_cylinder_ns(tmp_path, size):
+    """Laminar cylinder O-grid at Re 100, Ma 0.2, LSQ + Barth, Kutta RK3: 128 x 64 and the
+    full 512 x 256 (262,144 cells) workload of the Navier-Stokes bench line."""
+    import os
+    from oracle import pyoracle
+    tp, su2 = cases.cylinder_ns(str(tmp_path), *size)
     o = Oracle(tp, su2)
     s, p, _ = make(tp, su2)
     U0 = o.init_field()
     assert rel(s.rhs(U0), o.rhs(U0)[0]) <= 1e-12
-    U, t, _, _ = o.run(U0, 3)
+    before = pyoracle.set_threads(0)
+    pyoracle.set_threads(os.cpu_count() or 1)
+    try:
+        U, t, _, _ = o.run(U0, 3)
+    finally:
+        pyoracle.set_threads(before)
     s.set_state(U0)
     s.step(0.0, p.T_end, 3)
     assert rel(s.get_state(), U) <= 1e-11
