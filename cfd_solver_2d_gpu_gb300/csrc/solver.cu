@@ -199,7 +199,7 @@ int Solver::init(const fvgb_mesh_soa& m, const fvgb_params& prm) {
 
 Solver::~Solver() {
     release_output();
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    drop_graphs();
     if (h_state) cudaFreeHost(h_state);
     for (void* q : owned) cudaFree(q);
     if (stream) cudaStreamDestroy(stream);
@@ -313,20 +313,36 @@ int Solver::profile_steps(double T, int nsteps, double* ms, int* count) {
     return check_status();
 }
 
+void Solver::drop_graphs() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph_exec_multi) cudaGraphExecDestroy(graph_exec_multi);
+    graph_exec = graph_exec_multi = nullptr;
+}
+
+// The step captured once as a graph of one step and once as a graph of kGraphSteps
+// steps back to back: long runs replay the second, so a graph boundary (and its launch)
+// comes once every kGraphSteps steps instead of every step.
 int Solver::build_graph() {
-    if (graph_exec) return 0;
-    cudaGraph_t g = nullptr;
-    const long long before = launches;
-    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step();
-    cudaError_t e = cudaStreamEndCapture(stream, &g);
-    if (e != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    launches_per_step = launches - before;
-    launches = before;
-    e = cudaGraphInstantiate(&graph_exec, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    return 0;
+    if (graph_exec && graph_exec_multi) return 0;
+    drop_graphs();
+    auto capture = [&](int steps, cudaGraphExec_t* out) -> int {
+        cudaGraph_t g = nullptr;
+        const long long before = launches;
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < steps; i++) enqueue_step();
+        cudaError_t e = cudaStreamEndCapture(stream, &g);
+        if (e != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        if (steps == 1) launches_per_step = launches - before;
+        launches = before;
+        e = cudaGraphInstantiate(out, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        return 0;
+    };
+    int rc = capture(1, &graph_exec);
+    if (!rc) rc = capture(kGraphSteps, &graph_exec_multi);
+    if (rc) drop_graphs();
+    return rc;
 }
 
 int Solver::check_status() {
@@ -354,7 +370,9 @@ int Solver::step_async(double T, int nsteps) {
     int rc = build_graph();
     if (rc) return rc;
     CK(cudaMemcpyAsync(&d_state->T, &T, sizeof(double), cudaMemcpyHostToDevice, stream));
-    for (int i = 0; i < nsteps; i++) CK(cudaGraphLaunch(graph_exec, stream));
+    int i = 0;
+    for (; i + kGraphSteps <= nsteps; i += kGraphSteps) CK(cudaGraphLaunch(graph_exec_multi, stream));
+    for (; i < nsteps; i++) CK(cudaGraphLaunch(graph_exec, stream));
     launches += launches_per_step * nsteps;
     return 0;
 }
@@ -540,10 +558,7 @@ extern "C" int fvgb_set_cfl(fvgb_handle* h, double CFL) {
     if (s.p.CFL == CFL) return 0;
     CK(cudaStreamSynchronize(s.stream));  // no launch of the old graph is still pending
     s.p.CFL = CFL;
-    if (s.graph_exec) {  // the step was captured with the old value
-        cudaGraphExecDestroy(s.graph_exec);
-        s.graph_exec = nullptr;
-    }
+    s.drop_graphs();  // the step was captured with the old value
     return 0;
 }
 

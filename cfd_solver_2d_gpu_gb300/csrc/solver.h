@@ -21,7 +21,9 @@ struct Solver {
     Layout L;
     int N = 0, E = 0;
     cudaStream_t stream = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;        // one step
+    cudaGraphExec_t graph_exec_multi = nullptr;  // kGraphSteps steps in one graph
+    static constexpr int kGraphSteps = 8;
     std::vector<void*> owned;
     dev::Gas gas{};
     dev::BcData bc{};
@@ -86,6 +88,7 @@ struct Solver {
     void enqueue_stage(int kind);
     void enqueue_step();
     int build_graph();
+    void drop_graphs();
     int check_status();
     int step_async(double T, int nsteps);
     int set_time(double t);
