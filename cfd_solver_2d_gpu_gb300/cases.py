@@ -99,6 +99,38 @@ def square_mesh(n, jitter=0.0, L=10.0, seed=JITTER_SEED, directory=None):
     return path
 
 
+def mixed_mesh(su2_path, out_path, seed=5):
+    """A copy of a quad mesh in which a seeded half of the quads are written as two
+    triangles split along the other diagonal, (n0, n1, n2) + (n0, n2, n3), where the
+    reader itself splits a quad into (n0, n1, n3) + (n3, n1, n2): a mesh of mixed
+    element types and mixed diagonals."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    lines = open(su2_path).read().split("\n")
+    out, i = [], 0
+    while i < len(lines):
+        ln = lines[i]
+        if ln.startswith("NELEM="):
+            n = int(ln.split("=")[1])
+            elems = []
+            for q in lines[i + 1:i + 1 + n]:
+                f = q.split()
+                if f[0] == "9" and rng.random() < 0.5:
+                    a, b, c, d = f[1:5]
+                    elems += [f"5 {a} {b} {c}", f"5 {a} {c} {d}"]
+                else:
+                    elems.append(" ".join(f[:-1]))
+            out.append(f"NELEM= {len(elems)}")
+            out += [f"{e} {k}" for k, e in enumerate(elems)]
+            i += 1 + n
+            continue
+        out.append(ln)
+        i += 1
+    with open(out_path, "w") as fh:
+        fh.write("\n".join(out))
+    return out_path
+
+
 def channel_mesh(n, jitter=0.0, L=10.0, seed=JITTER_SEED, directory=None):
     """The square of square_mesh with its four boundaries renamed: inlet (x = 0),
     outlet (x = L), symmetry (y = L) and wall (y = 0; slip for Euler, no-slip

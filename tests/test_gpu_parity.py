@@ -302,6 +302,28 @@ def test_bad_mesh_indices_are_refused(tmp_path):
         assert rc == -4 and "outside" in fv.lib().fvgb_last_error().decode(), name
 
 
+@pytest.mark.parametrize("base", ["channel", "square"])
+def test_mixed_element_mesh_matches_the_oracle(tmp_path, base):
+    """Triangles and quads in one file (half of the quads written as two triangles on the
+    other diagonal): residual and 5 SSP-RK3 steps, second order, against the oracle."""
+    src = (cases.channel_mesh if base == "channel" else cases.square_mesh)(16, jitter=0.2, directory=str(tmp_path))
+    su2 = cases.mixed_mesh(src, str(tmp_path / f"mixed_{base}.su2"))
+    tp = str(tmp_path / "mixed.toml")
+    extra = dict(vortex=(2.5, 7.0, 3.0), inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0),
+                 outlet=(1.0, 1.0, 0.0, 0.9)) if base == "channel" else {}
+    with open(tp, "w") as f:
+        f.write(cases.toml_text(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.6,
+                                **extra))
+    s, p, m = make(tp, su2)
+    o = Oracle(tp, su2)
+    U0 = cases.wavy(m, o.init_field())
+    assert rel(s.rhs(U0), o.rhs(U0)[0]) <= 1e-12
+    U, _, _, _ = o.run(U0, 5)
+    s.set_state(U0)
+    s.step(0.0, p.T_end, 5)
+    assert rel(s.get_state(), U) <= 1e-10
+
+
 @pytest.mark.parametrize("kind", ["square2", "square3", "channel2"])
 @pytest.mark.parametrize("second_order", [False, True])
 def test_tiny_meshes_match_the_oracle(tmp_path, kind, second_order):

@@ -205,6 +205,27 @@ def test_steady_inputs(tmp_path):
     assert "is_steady" in str(e.value)
 
 
+@pytest.mark.parametrize("base", ["channel", "square"])
+def test_mixed_element_mesh_matches_the_oracle_reader(tmp_path, base):
+    """Triangles and quads in one file (half of the quads written as two triangles on the
+    other diagonal): this library's O(N) reader gives the oracle's arrays, which follow the
+    reference's legacy assembly, bit for bit."""
+    from oracle.pyoracle import Oracle
+    src = (cases.channel_mesh if base == "channel" else cases.square_mesh)(10, jitter=0.2, directory=str(tmp_path))
+    su2 = cases.mixed_mesh(src, str(tmp_path / f"mixed_{base}.su2"))
+    assert "\n5 " in open(su2).read() and "\n9 " in open(su2).read()
+    tp, _ = cases.vortex_small(str(tmp_path), n=4)
+    p = fv.Params.from_toml(tp)
+    m = fv.Mesh.read_su2(su2, p)
+    o = Oracle(tp, su2)
+    assert (m.N, m.E) == (o.N, o.E)
+    for mine, theirs in (("elem_edges", "elem_edges"), ("elem_nodes", "elem_nodes"),
+                         ("elem_neighbors", "elem_nbrs"), ("edge_L", "edge_L"), ("edge_R", "edge_R"),
+                         ("edge_setID", "edge_set"), ("elem_volume", "elem_vol"), ("elem_xy", "elem_xy")):
+        a, b = np.asarray(m.array(mine)), o.array(theirs)
+        assert np.array_equal(a.reshape(b.shape), b), mine
+
+
 def test_create_refuses_bad_meshes_on_the_host(tmp_path):
     """fvgb_create checks the caller's mesh before it looks for a device: an empty mesh,
     a NULL array and an index outside the mesh are FVGB_ERR_MESH (-4) here, without a
