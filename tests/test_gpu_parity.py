@@ -302,18 +302,22 @@ def test_bad_mesh_indices_are_refused(tmp_path):
         assert rc == -4 and "outside" in fv.lib().fvgb_last_error().decode(), name
 
 
-@pytest.mark.parametrize("base", ["channel", "square"])
-def test_mixed_element_mesh_matches_the_oracle(tmp_path, base):
+@pytest.mark.parametrize("base,scheme", [("channel", "euler_lsq_roe"), ("square", "euler_lsq_roe"),
+                                         ("channel", "ns_gg_llf"), ("square", "ns_lsq_roe")])
+def test_mixed_element_mesh_matches_the_oracle(tmp_path, base, scheme):
     """Triangles and quads in one file (half of the quads written as two triangles on the
-    other diagonal): residual and 5 SSP-RK3 steps, second order, against the oracle."""
+    other diagonal): residual and 5 SSP-RK3 steps, second order, against the oracle; Euler
+    and laminar Navier-Stokes (Re 100), least squares and Green-Gauss, Roe and LLF."""
     src = (cases.channel_mesh if base == "channel" else cases.square_mesh)(16, jitter=0.2, directory=str(tmp_path))
     su2 = cases.mixed_mesh(src, str(tmp_path / f"mixed_{base}.su2"))
     tp = str(tmp_path / "mixed.toml")
     extra = dict(vortex=(2.5, 7.0, 3.0), inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0),
                  outlet=(1.0, 1.0, 0.0, 0.9)) if base == "channel" else {}
+    extra.update({"euler_lsq_roe": dict(flux=2002, gradient=1),
+                  "ns_gg_llf": dict(equation=2, Re=100.0, flux=2001, gradient=2),
+                  "ns_lsq_roe": dict(equation=2, Re=100.0, flux=2002, gradient=1)}[scheme])
     with open(tp, "w") as f:
-        f.write(cases.toml_text(flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.6,
-                                **extra))
+        f.write(cases.toml_text(reconstruct=3002, limiter=1, time_advance=3104, CFL=0.6, **extra))
     s, p, m = make(tp, su2)
     o = Oracle(tp, su2)
     U0 = cases.wavy(m, o.init_field())
