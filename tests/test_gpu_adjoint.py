@@ -281,7 +281,7 @@ def test_adjoint_navier_stokes(tmp_path, kind):
 
 
 @pytest.mark.parametrize("kind", ["vortex_lsq_barth_roe", "vortex_gg_llf", "vortex_o1", "channel_subsonic",
-                                  "vortex_ns", "channel_ns_gg", "vortex_steady"])
+                                  "vortex_ns", "channel_ns_gg", "vortex_steady", "channel_mixed"])
 def test_rhs_vjp_matches_fd(tmp_path, kind):
     """fvgb_rhs_vjp, (dR/dU)^T seed, against central finite differences of fvgb_rhs
     (seed . (R(U + h d) - R(U - h d)) / 2h against d . grad, random unit directions d)."""
@@ -292,13 +292,16 @@ def test_rhs_vjp_matches_fd(tmp_path, kind):
         su2 = cases.square_mesh(16, jitter=0.2, directory=d)
     else:
         su2 = cases.channel_mesh(12, jitter=0.2, directory=d)
+    if kind == "channel_mixed":  # triangles and quads in one file
+        su2 = cases.mixed_mesh(su2, str(tmp_path / "mixed.su2"))
     cfg = {"vortex_lsq_barth_roe": dict(flux=2002, reconstruct=3002, gradient=1, limiter=1),
            "vortex_gg_llf": dict(flux=2001, reconstruct=3002, gradient=2, limiter=1),
            "vortex_o1": dict(flux=2002, reconstruct=3001, gradient=1, limiter=1),
            "channel_subsonic": dict(flux=2002, reconstruct=3002, gradient=1, limiter=1, **channel),
            "vortex_ns": dict(equation=2, flux=2002, reconstruct=3002, gradient=1, limiter=1, Re=100.0),
            "channel_ns_gg": dict(equation=2, flux=2002, reconstruct=3002, gradient=2, limiter=1, Re=100.0, **channel),
-           "vortex_steady": dict(flux=2002, reconstruct=3002, gradient=1, limiter=1, steady=1)}[kind]
+           "vortex_steady": dict(flux=2002, reconstruct=3002, gradient=1, limiter=1, steady=1),
+           "channel_mixed": dict(flux=2002, reconstruct=3002, gradient=1, limiter=1, **channel)}[kind]
     text = cases.toml_text(time_advance=3104, CFL=0.6, **cfg)
     p, solver, U0, _ = boundary_case(tmp_path, kind, text, su2)
     rng = np.random.default_rng(5)

@@ -60,6 +60,25 @@ def test_batch_matches_plain_vortex_ssp_gg_llf(tmp_path):
         assert np.array_equal(b.get_state(i), U), i
 
 
+def test_batch_matches_plain_mixed_elements(tmp_path):
+    """Instances whose meshes mix triangles and quads (half of the quads written as two
+    triangles on the other diagonal) next to plain quad meshes."""
+    inst = []
+    for i, (n, mixed) in enumerate(((10, True), (14, False), (12, True))):
+        src = cases.channel_mesh(n, jitter=0.2, directory=str(tmp_path))
+        sp = cases.mixed_mesh(src, str(tmp_path / f"mx{i}.su2"), seed=i) if mixed else src
+        tp, _ = cases.write_case(str(tmp_path), f"mx{i}", cases.toml_text(
+            flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104, CFL=0.6, vortex=(2.5, 7.0, 3.0),
+            inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0), outlet=(1.0, 1.0, 0.0, 0.9)), sp)
+        inst.append(load(tp, sp))
+    b = fv.Batch([m for m, _ in inst], [p for _, p in inst])
+    t = b.step(3)
+    for i, (m, p) in enumerate(inst):
+        U, tp = plain_run(m, p, 3)
+        assert np.array_equal(b.get_state(i), U), i
+        assert t[i] == tp
+
+
 def test_batch_matches_plain_channels(tmp_path):
     """Inlet, outlet, symmetry and slip-wall edges, each instance with its own inflow and
     outflow states (one supersonic)."""
