@@ -19,8 +19,6 @@
 // needed between calls.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "internal.h"
 #include "solver.h"
 
@@ -28,27 +26,20 @@ namespace fvgb {
 namespace {
 
 constexpr int kNoallocMaxEdges = 1 << 20;   // 1,048,576 edges -> 4 doubles each = 32 MiB
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_edge_flux[4 * (size_t)kNoallocMaxEdges];
 
-// host-side addresses of the array, looked up once per device with that device current
-// (in host code the array's name is only a stand-in, never a device address); the
-// first call on a device does this look-up, so it belongs before any stream capture
-std::mutex g_addr_mu;
-double* g_addr[kMaxDevices] = {};
-
-int scratch_address(int device, double** out) {
-    if (device < 0 || device >= kMaxDevices) return fail(FVGB_ERR_ARG, "device ordinal out of range");
-    std::lock_guard<std::mutex> lk(g_addr_mu);
-    if (!g_addr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_edge_flux);
-        if (e != cudaSuccess)
-            return fail(FVGB_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_addr[device] = static_cast<double*>(p);
-    }
-    *out = g_addr[device];
+// The array's device address in the context current on the calling thread.  In host code
+// the array's name is only a stand-in, never a device address, so every call asks the
+// runtime for it (cudaGetSymbolAddress allocates nothing).  Nothing is cached: a cached
+// address would go stale after cudaDeviceReset or when the caller switches to another
+// context on the same device.  The first call in a context also loads the library's
+// device code there, which is why that first call belongs before any stream capture.
+int scratch_address(double** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_edge_flux);
+    if (e != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    *out = static_cast<double*>(p);
     return 0;
 }
 
@@ -156,11 +147,8 @@ extern "C" int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params
             (e && !d.boundary_type))
             return fail(FVGB_ERR_ARG, "fvgb_rhs_noalloc: a mesh array it reads is NULL");
     }
-    int device = 0;
-    cudaError_t e = cudaGetDevice(&device);
-    if (e != cudaSuccess) return fail(FVGB_ERR_CUDA, cudaGetErrorString(e));
     double* F = nullptr;
-    int rc = scratch_address(device, &F);
+    int rc = scratch_address(&F);
     if (rc) return rc;
     RefMesh m;
     m.N = dev_mesh->num_element;
@@ -184,7 +172,7 @@ extern "C" int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params
         else k_noalloc_flux<2001><<<b, 256, 0, s>>>(m, U_dev, g, bc, p->dsr_time, F);
     }
     if (m.N > 0) k_noalloc_gather<<<(m.N + 255) / 256, 256, 0, s>>>(m, F, rhs_dev);
-    e = cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("fvgb_rhs_noalloc launch: ") + cudaGetErrorString(e));
     return 0;
 }

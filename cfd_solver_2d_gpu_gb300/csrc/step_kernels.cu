@@ -151,6 +151,12 @@ __global__ void __launch_bounds__(256) k_gather_out(const d4* __restrict__ U, do
     dst[3 * (size_t)N + r] = u.w;
 }
 
+// the larger of two norms, NaN if either is NaN.  The reference's Math::max ((a > b) ? a : b,
+// FVMR/src/math/BasicAlgorithm.h:10-12) lets a NaN through only when it comes last in its cell
+// order; here any NaN residual gives a NaN norm, so that the driver's isnan stop
+// (CDriver.cpp:235-263) fires whatever the cell order.
+__device__ __forceinline__ double max_nan(double a, double b) { return (is_nan(a) || is_nan(b)) ? a + b : fmax(a, b); }
+
 // get_residual_host (FVMR/src/output/residual/Residual.cpp:4-43): per-block
 // partial norms, then one block combines them in a fixed order (deterministic)
 __global__ void __launch_bounds__(256) k_residual_partial(const d4* __restrict__ R, int N, int norm,
@@ -168,7 +174,8 @@ __global__ void __launch_bounds__(256) k_residual_partial(const d4* __restrict__
     for (int s = blockDim.x / 2; s > 0; s >>= 1) {
         if ((int)threadIdx.x < s) {
             d4 x = sm[threadIdx.x], y = sm[threadIdx.x + s];
-            if (norm == 0) sm[threadIdx.x] = mk4(fmax(x.x, y.x), fmax(x.y, y.y), fmax(x.z, y.z), fmax(x.w, y.w));
+            if (norm == 0)
+                sm[threadIdx.x] = mk4(max_nan(x.x, y.x), max_nan(x.y, y.y), max_nan(x.z, y.z), max_nan(x.w, y.w));
             else sm[threadIdx.x] = mk4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
         }
         __syncthreads();
@@ -181,7 +188,7 @@ __global__ void k_residual_final(const d4* __restrict__ part, int nb, int norm, 
     d4 a = mk4(0, 0, 0, 0);
     for (int i = 0; i < nb; i++) {
         d4 y = part[i];
-        if (norm == 0) a = mk4(fmax(a.x, y.x), fmax(a.y, y.y), fmax(a.z, y.z), fmax(a.w, y.w));
+        if (norm == 0) a = mk4(max_nan(a.x, y.x), max_nan(a.y, y.y), max_nan(a.z, y.z), max_nan(a.w, y.w));
         else a = mk4(a.x + y.x, a.y + y.y, a.z + y.z, a.w + y.w);
     }
     if (norm == 2) a = mk4(sqrt(a.x), sqrt(a.y), sqrt(a.z), sqrt(a.w));

@@ -345,10 +345,12 @@ int fvgb_batch_info(fvgb_batch* b, long long out[8]);
  * stream); the call only enqueues work.  The edge fluxes are kept in one
  * library-wide device array of 32 MiB (at most 1,048,576 edges; larger meshes
  * get FVGB_ERR_ARG).  Every call shares that array, so calls that overlap
- * on the GPU race on it and must be serialised by the caller.  The first call
- * on each device, with that device current, looks up the array's device
- * address (cudaGetSymbolAddress: a runtime query, no allocation); make that
- * first call before any stream capture begins.  Far-field ghost states out of
+ * on the GPU race on it and must be serialised by the caller.  Every call
+ * looks up the array's device address in the current context
+ * (cudaGetSymbolAddress: a runtime query, no allocation; nothing is cached,
+ * so a device reset or a switch of context is safe); the first call in a
+ * context also loads the library's device code there, so make that first
+ * call before any stream capture begins.  Far-field ghost states out of
  * range are not reported by this call. */
 int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params* p, const double* U_dev, double* rhs_dev,
                      void* stream);

@@ -28,7 +28,8 @@
 //   continue   the newest pause_<basic.filename>[n].dat of the folder given in
 //              place of the mesh, read by ContinueFileReader::readContinueFile_1
 //              (FVMR/src/input/ContinueFileReader.cpp:19-158): mesh and field only
-// and writes every SoA array, the final field and the per-step dt to a small
+// and writes every SoA array, the final field, the per-step dt and the residual
+// norms of the last residual (get_residual_host, all three norms) to a small
 // binary file ("FVMRDUMP" + named arrays) that tests read with numpy.
 #include <cstdio>
 #include <cstdlib>
@@ -104,6 +105,22 @@ void residual(GPU::GPUSolver2& s, const std::vector<double>& U, std::vector<doub
     load_field(U, s.elementField_host.U, n);
     U2NITS::Time::calculateFunctionF(s.element_host, s.node_host, s.edge_host, s.elementField_host);
     copy_field(s.elementField_host.Flux, R, n);
+}
+
+// The reference's own residual norms of the singleton's last residual (elementField_host.Flux),
+// U2NITS::Output::get_residual_host (FVMR/src/output/residual/Residual.cpp:4-43), as
+// GPUSolver2::updateResidualVector (GPUSolver2.cpp:294-296) asks for them: rows L-infinity,
+// L1, L2 (the NormType order), columns the four conserved variables.
+std::vector<double> residual_norms(GPU::GPUSolver2& s) {
+    std::vector<double> out;
+    const U2NITS::Output::NormType kinds[3] = {U2NITS::Output::normType_infinity, U2NITS::Output::normType_1,
+                                               U2NITS::Output::normType_2};
+    for (U2NITS::Output::NormType k : kinds) {
+        myfloat r[4] = {0, 0, 0, 0};
+        U2NITS::Output::get_residual_host(s.elementField_host, r, k);
+        for (int v = 0; v < 4; v++) out.push_back((double)r[v]);
+    }
+    return out;
 }
 
 myfloat global_dt(GPU::GPUSolver2& s) {
@@ -190,6 +207,7 @@ int main(int argc, char** argv) {
         std::vector<double> alpha(s.elementFieldVariable_dt_host.alphaC, s.elementFieldVariable_dt_host.alphaC + N);
         residual(s, U0, R);
         d.f64("rhs", R);
+        d.f64("residual_norms", residual_norms(s));
         d.rows("grad_x", s.elementField_host.Ux, 4, N);
         d.rows("grad_y", s.elementField_host.Uy, 4, N);
         d.f64("dt", dt);
@@ -254,6 +272,7 @@ int main(int argc, char** argv) {
         U2NITS::Space::Restrict::modifyElementFieldU2d(s.element_host, s.elementField_host);
     }
     d.rows("U", s.elementField_host.U, 4, N);
+    d.f64("residual_norms", residual_norms(s));
     if (mode == "output") {
         // the writers read ruvp: refresh it from the final state
         CIteration::update_host_ruvp_Uold(s.elementField_host.U, s.elementField_host.ruvp, s.elementField_host.Uold, N,

@@ -7,8 +7,10 @@ Run here, where the reference sources are present:
 
 Each fixture is one compressed .npz with the case's input.toml text, the mesh
 (.su2 text, compressed), the reference's mesh arrays, its initial field, one
-residual evaluation (rhs, limited gradients, dt) and the state after a few
-steps.  Test infrastructure.
+residual evaluation (rhs, limited gradients, dt), the state after a few
+steps, and the reference's residual norms (get_residual_host: L-infinity, L1
+and L2) of the rhs evaluation and of the last residual of the steps.  Test
+infrastructure.
 """
 import gzip
 import io
@@ -219,7 +221,11 @@ def main(only=()):
                        U=stp["U"], dts=stp["dts"], t=stp["t"], steps=np.array([steps]),
                        toml=np.frombuffer(toml.encode(), dtype=np.uint8),
                        su2_gz=np.frombuffer(gzip.compress(open(su2, "rb").read(), mtime=0), dtype=np.uint8),
-                       mode=np.frombuffer(mode.encode(), dtype=np.uint8))
+                       mode=np.frombuffer(mode.encode(), dtype=np.uint8),
+                       # the reference's get_residual_host norms (rows L-inf, L1, L2) of the rhs
+                       # evaluation and of the last residual the steps evaluated
+                       residual_rhs=rhs["residual_norms"].reshape(3, 4),
+                       residual_step=stp["residual_norms"].reshape(3, 4))
             if os.path.exists(REF32):  # the reference as shipped (float), for the record
                 s32 = run_ref(REF32, tp, su2, mode, steps, os.path.join(d, name + "_f32.bin"))
                 out["U_f32"] = s32["U"]

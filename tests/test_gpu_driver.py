@@ -13,6 +13,7 @@ import pytest
 
 import cfd_solver_2d_gpu_gb300 as fv
 from cfd_solver_2d_gpu_gb300 import cases
+from oracle.pyoracle import Oracle
 
 pytestmark = pytest.mark.gpu
 EXE = os.path.join(os.path.dirname(fv.__file__), "fvgb_run")
@@ -55,6 +56,12 @@ def test_driver_matches_direct_stepping(tmp_path):
     assert hist[2].startswith("zone")
     rows = [l.split() for l in hist[3:] if l]
     assert [int(r[0]) for r in rows] == [1, 5, 10, 15, 20, 25, 30] and all(len(r) == 8 for r in rows)
+    # the residual columns: the L-infinity norms of updateResidualVector (GPUSolver2.cpp:294-296),
+    # against the oracle's get_residual_host of its own last residual after 30 steps, to the
+    # precision of the file's %e (6 significant decimals)
+    o = Oracle(tp, os.path.join(d, "jv.su2"))
+    _, _, _, last = o.run(o.init_field(), 30)
+    assert np.allclose([float(x) for x in rows[-1][2:6]], o.residual(last, 0), rtol=1e-6, atol=0)
     assert "step = 10" in r.stdout and "step = 30" in r.stdout
     # Tecplot volume files at step 1 and at the stop, the boundary file overwritten in place
     out = os.path.join(d, "out")

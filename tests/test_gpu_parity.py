@@ -71,6 +71,49 @@ def test_steps_match_reference(golden):
     assert abs(t - g["t"][0]) <= 1e-11 * g["t"][0]
 
 
+def test_residual_norms_match_reference(golden):
+    """fvgb_residual, the replacement of GPUSolver2::updateResidualVector over
+    get_residual_host (FVMR/src/output/residual/Residual.cpp:4-43), against the
+    reference's own norms (L-infinity, L1, L2) stored in the fixture: of one residual
+    evaluation, at 1e-12; and of the last residual of the fixture's steps (Euler, Kutta
+    RK3, SSP-RK3 and steady runs), at the tolerance of the state after those steps scaled
+    by the residual's sensitivity (the residual of a state that differs by d differs by
+    about d / h), and against the oracle's norms of the oracle's last residual, which the
+    oracle computes the reference's way, at the same tolerance."""
+    name, (tp, sp, g) = golden
+    s, p, m = make(tp, sp)
+    s.rhs(g["U0"])
+    for norm in (0, 1, 2):
+        assert rel(s.update_residual_vector(norm), g["residual_rhs"][norm]) <= 1e-12, (name, norm)
+    n = int(g["steps"][0])
+    s.set_state(g["U0"])
+    s.step(0.0, p.T_end, n)
+    o = Oracle(tp, sp)
+    _, _, _, last = o.run(g["U0"], n)
+    tol = 1e-7 if n >= 1000 else (1e-8 if p.reconstruct == 3002 else 1e-10)
+    for norm in (0, 1, 2):
+        got = s.update_residual_vector(norm)
+        assert rel(got, g["residual_step"][norm]) <= tol, (name, norm, rel(got, g["residual_step"][norm]))
+        assert np.array_equal(o.residual(last, norm), g["residual_step"][norm]) or \
+            rel(o.residual(last, norm), g["residual_step"][norm]) <= 1e-14, (name, norm)
+
+
+def test_residual_norm_is_nan_when_a_residual_is(tmp_path):
+    """A NaN anywhere in the residual makes the L-infinity norm NaN, whichever cell holds it,
+    so that the driver's NaN stop (CDriver.cpp:235-263) fires; L1 and L2 sums carry it too."""
+    tp, su2 = cases.vortex_small(str(tmp_path), n=32)
+    s, p, m = make(tp, su2)
+    U = s.get_state()
+    for cell in (0, m.N // 2, m.N - 1):
+        V = U.copy()
+        V[1, cell] = np.nan
+        s.rhs(V)
+        for norm in (0, 1, 2):
+            assert np.isnan(s.update_residual_vector(norm)[1]), (cell, norm)
+    s.rhs(U)
+    assert np.all(np.isfinite(s.update_residual_vector(0)))
+
+
 def test_connectivity_maps_back_bit_exact(golden):
     name, (tp, sp, g) = golden
     s, p, m = make(tp, sp, renumber=1)
@@ -244,6 +287,32 @@ def test_full_size_step_matches_the_oracle(tmp_path):
     tg = s.step(0.0, p.T_end, 1)
     assert abs(tg - t) <= 1e-12 * t
     assert rel(s.get_state(), U) <= 1e-12
+
+
+@pytest.mark.parametrize("flux", [2002, 2001])
+def test_full_size_200_steps_match_the_oracle(tmp_path, flux):
+    """The large plain configuration at its own horizon: 1448x1448 jittered vortex
+    (4,193,408 cells), LSQ + Barth, Roe and LLF, SSP-RK3, CFL 0.8, 200 steps on the GPU
+    against 200 steps of the oracle on all host threads (about a minute on 16 cores).
+    The bound is the 1000-step tolerance, 1e-9; the measured drift is printed."""
+    import os
+    from oracle import pyoracle
+    tp, su2 = cases.vortex_large(str(tmp_path), flux=flux)
+    before = pyoracle.set_threads(0)
+    pyoracle.set_threads(os.cpu_count() or 1)
+    try:
+        o = Oracle(tp, su2)
+        U0 = o.init_field()
+        U, t, _, _ = o.run(U0, 200)
+    finally:
+        pyoracle.set_threads(before)
+    s, p, m = make(tp, su2)
+    s.set_state(U0)
+    tg = s.step(0.0, p.T_end, 200)
+    drift = rel(s.get_state(), U)
+    print(f"1448^2 flux {flux}: t = {t:.6f}, drift after 200 steps {drift:.3e}")
+    assert abs(tg - t) <= 1e-11 * t
+    assert drift <= 1e-9, drift
 
 
 def test_large_mesh_properties(tmp_path):

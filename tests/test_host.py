@@ -61,7 +61,10 @@ def test_toml_matches_reference_semantics(name):
         assert np.allclose(list(getattr(p, k)), list(getattr(q, k)), rtol=1e-15, atol=0), k
 
 
-REF_TOML = "/root/reference/quick_start/U2NITS-10.0"
+# the reference's example cases, reached through the link the oracle recipe (oracle/ref) makes
+# next to the reference build where the reference tree is mounted
+REF_TOML = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "quick_start",
+                        "U2NITS-10.0")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_TOML), reason="reference tree not mounted")
@@ -94,6 +97,17 @@ def test_su2_writers(tmp_path):
     assert m.N == 128 and sorted(m.array("boundary_type")) == [6002, 6013]
     r = np.hypot(*m.array("node_xy"))
     assert np.isclose(r.min(), 0.5) and np.isclose(r.max(), 20.0)
+
+
+@pytest.mark.parametrize("n,jitter,seed", [(8, 0.2, 7), (24, 0.2, 20261203), (5, 0.0, 1), (2, 0.3, 3)])
+def test_python_square_writer_is_byte_identical(tmp_path, n, jitter, seed):
+    """oracle/meshgen.py (numpy only; the reference arm of bench.py makes its mesh with it,
+    so that it never loads the CUDA library) writes the library writer's exact bytes."""
+    from oracle import meshgen
+    a, b = str(tmp_path / "lib.su2"), str(tmp_path / "py.su2")
+    fv.write_periodic_square(a, n, 10.0, jitter, seed)
+    meshgen.write_periodic_square(b, n, 10.0, jitter, seed)
+    assert open(a, "rb").read() == open(b, "rb").read()
 
 
 def test_errors_are_codes_not_exits(tmp_path):

@@ -4,8 +4,9 @@ own memory arena, or a path that cannot take the device-wide pause an
 allocation can cause).  The test plays such a caller: it places the
 reference-layout arrays on the GPU itself, calls the entry point through the
 C ABI twice in a row on different states, and compares each result with the
-ordinary residual entry point (fvgb_rhs) at the parity tolerance (1e-12,
-relative L-infinity).  The file sorts last so a failure here comes after every
+ordinary residual entry point (fvgb_rhs) and with the oracle's residual (the
+C restatement of the reference's calculateFunctionF) at the parity tolerance
+(1e-12, relative L-infinity).  The file sorts last so a failure here comes after every
 other test has run."""
 import ctypes
 
@@ -14,6 +15,7 @@ import pytest
 
 import cfd_solver_2d_gpu_gb300 as fv
 from cfd_solver_2d_gpu_gb300 import cases
+from oracle.pyoracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -38,7 +40,7 @@ def device_mesh(mesh):
     return soa, keep
 
 
-@pytest.mark.parametrize("kind", ["vortex_roe", "cylinder_llf", "dmr_roe"])
+@pytest.mark.parametrize("kind", ["vortex_roe", "cylinder_llf", "dmr_roe", "mixed_channel_llf"])
 def test_rhs_noalloc_matches_rhs(tmp_path, kind):
     import torch
     L = fv.lib()
@@ -53,13 +55,21 @@ def test_rhs_noalloc_matches_rhs(tmp_path, kind):
             f.write(cases.toml_text(equation=1, flux=2001, reconstruct=3001, gradient=1, limiter=1,
                                     time_advance=3103, CFL=0.5, ic_type=1, inf_mode=0, Ma=0.5))
         su2 = cases.cylinder_mesh(64, 32, directory=str(tmp_path))
-    else:  # double Mach reflection: "dsr" edges at p.dsr_time against the handle's clock
+    elif kind == "dmr_roe":  # double Mach reflection: "dsr" edges at p.dsr_time against the handle's clock
         tp = str(tmp_path / "dmr.toml")
         with open(tp, "w") as f:
             f.write(cases.toml_text(equation=1, flux=2002, reconstruct=3001, gradient=1, limiter=1,
                                     time_advance=3101, CFL=0.5, ic_type=4, dmr=(1.0 / 6.0, 0.0, 60.0),
                                     inlet=(8.0, 8.25, -30.0, 116.5, "angle"), outlet=(1.4, 0.0, 0.0, 1.0)))
         su2 = cases.dmr_mesh(48, jitter=0.2, directory=str(tmp_path))
+    else:  # triangles and quads in one file, first order, LLF
+        src = cases.channel_mesh(16, jitter=0.2, directory=str(tmp_path))
+        su2 = cases.mixed_mesh(src, str(tmp_path / "mixed_channel.su2"))
+        tp = str(tmp_path / "mixed.toml")
+        with open(tp, "w") as f:
+            f.write(cases.toml_text(flux=2001, reconstruct=3001, time_advance=3104, CFL=0.6, vortex=(2.5, 7.0, 3.0),
+                                    inf=(1.0, 1.0, 0.3, 1.0), inlet=(1.0, 1.0, 0.3, 1.0),
+                                    outlet=(1.0, 1.0, 0.0, 0.9)))
     p = fv.Params.from_toml(tp)
     mesh = fv.Mesh.read_su2(su2, p)
     solver = fv.GPUSolver2(mesh, p)
@@ -69,6 +79,8 @@ def test_rhs_noalloc_matches_rhs(tmp_path, kind):
     p.dsr_time = t  # the handle's clock after the steps
     U1 = solver.get_state()
     soa, keep = device_mesh(mesh)
+    o = Oracle(tp, su2)
+    o.params.dsr_time = t
     stream = torch.cuda.current_stream().cuda_stream
     for U in (U0, U1):  # two calls in a row share the library's edge-flux array
         Ud = torch.from_numpy(np.ascontiguousarray(U)).cuda()
@@ -77,7 +89,9 @@ def test_rhs_noalloc_matches_rhs(tmp_path, kind):
         assert rc == 0, L.fvgb_last_error().decode()
         torch.cuda.synchronize()
         ref = solver.rhs(U)
-        assert rel(Rd.cpu().numpy(), ref) <= 1e-12
+        got = Rd.cpu().numpy()
+        assert rel(got, ref) <= 1e-12
+        assert rel(got, o.rhs(U)[0]) <= 1e-12
     if kind == "dmr_roe":  # the time matters: at t = 0 the tenth top edge is still downstream (outlet state)
         p.dsr_time = 0.0
         rc = L.fvgb_rhs_noalloc(ctypes.byref(soa), ctypes.addressof(p), Ud.data_ptr(), Rd.data_ptr(), stream)
