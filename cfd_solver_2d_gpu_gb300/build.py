@@ -48,6 +48,8 @@ def build(verbose=False, force=False):
               "-I", os.path.join(ROOT, "include"), "-I", CSRC] + ARCH
     if os.environ.get("FVGB_PTXAS_VERBOSE"):
         common += ["-Xptxas", "-v"]
+    # extra nvcc flags, e.g. -DFVGB_SOFT_MUL=0 (plain products on the FP64 pipe, for side-by-side timing)
+    common += os.environ.get("FVGB_NVCC_EXTRA", "").split()
 
     def compile_one(src):
         obj = os.path.join(OBJ, os.path.basename(src) + ".o")

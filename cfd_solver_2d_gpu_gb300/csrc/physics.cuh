@@ -11,6 +11,16 @@
 #include <cuda_runtime.h>
 
 #include "bc_types.h"
+#include "softfp64.cuh"
+
+// Where the kernels multiply (a plain product, not a fused multiply-add), they call mul():
+// the correctly rounded product computed on the integer pipes (softfp64.cuh), which run
+// beside the FP64 pipe that bounds these kernels on GB300.  The result is the IEEE
+// product bit for bit either way; FVGB_SOFT_MUL=0 at build time puts the products back on
+// the FP64 pipe (the same bits, for side-by-side timing).
+#ifndef FVGB_SOFT_MUL
+#define FVGB_SOFT_MUL 1
+#endif
 
 namespace fvgb {
 
@@ -63,6 +73,15 @@ __device__ __forceinline__ bool is_nan(double x) {
     return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
 
+// a * b, rounded once to nearest even, never contracted into a fused multiply-add
+__device__ __forceinline__ double mul(double a, double b) {
+#if FVGB_SOFT_MUL
+    return soft::dmul(a, b);
+#else
+    return __dmul_rn(a, b);
+#endif
+}
+
 // 1/x: the hardware's approximate reciprocal y (relative error e = 1 - x y,
 // |e| < 2^-22) refined by the cubic series 1/x = y (1 + e + e^2 + O(e^3)), one
 // fused multiply-add fewer than two Newton steps for the same accuracy: the
@@ -82,9 +101,9 @@ __device__ __forceinline__ Prim to_prim(const d4 U, const Gas& g) {
     Prim w;
     w.ir = rcp(U.x);
     w.r = U.x;
-    w.u = U.y * w.ir;
-    w.v = U.z * w.ir;
-    w.p = g.ga1 * fma(-0.5, fma(U.y, w.u, U.z * w.v), U.w);
+    w.u = mul(U.y, w.ir);
+    w.v = mul(U.z, w.ir);
+    w.p = mul(g.ga1, fma(-0.5, fma(U.y, w.u, mul(U.z, w.v)), U.w));
     return w;
 }
 
@@ -127,49 +146,49 @@ struct RoeRec {
 template <bool REC>
 __device__ __forceinline__ d4 roe_core(const Prim& L, const Prim& R, const d4 UL, const d4 UR, double nx, double ny,
                                        double area, const Gas& g, RoeRec* rec) {
-    const double ruL = fma(nx, UL.y, ny * UL.z), ruR = fma(nx, UR.y, ny * UR.z);
-    const double HL = (UL.w + L.p) * L.ir, HR = (UR.w + R.p) * R.ir;
+    const double ruL = fma(nx, UL.y, mul(ny, UL.z)), ruR = fma(nx, UR.y, mul(ny, UR.z));
+    const double HL = mul(UL.w + L.p, L.ir), HR = mul(UR.w + R.p, R.ir);
     const double psum = L.p + R.p;
     // central part 0.5 (F_L + F_R).n, scaled by 0.5 area at the end
-    d4 F = mk4(ruL + ruR, fma(ruL, L.u, fma(ruR, R.u, nx * psum)), fma(ruL, L.v, fma(ruR, R.v, ny * psum)),
-               fma(ruL, HL, ruR * HR));
+    d4 F = mk4(ruL + ruR, fma(ruL, L.u, fma(ruR, R.u, mul(nx, psum))), fma(ruL, L.v, fma(ruR, R.v, mul(ny, psum))),
+               fma(ruL, HL, mul(ruR, HR)));
     // Roe averages: rm = sqrt(rR rL), rrorl = sqrt(rR/rL) = rR / rm
-    const double prod = R.r * L.r;
+    const double prod = mul(R.r, L.r);
     const double irm = rsqrt(prod);
-    const double rm = prod * irm;
-    const double rrorl = R.r * irm;
+    const double rm = mul(prod, irm);
+    const double rrorl = mul(R.r, irm);
     const double w = rcp(rrorl + 1.0);
-    const double um = fma(R.u, rrorl, L.u) * w;
-    const double vm = fma(R.v, rrorl, L.v) * w;
-    const double Hm = fma(HR, rrorl, HL) * w;
-    const double Vm2 = fma(um, um, vm * vm);
-    const double am2 = g.ga1 * fma(-0.5, Vm2, Hm);
+    const double um = mul(fma(R.u, rrorl, L.u), w);
+    const double vm = mul(fma(R.v, rrorl, L.v), w);
+    const double Hm = mul(fma(HR, rrorl, HL), w);
+    const double Vm2 = fma(um, um, mul(vm, vm));
+    const double am2 = mul(g.ga1, fma(-0.5, Vm2, Hm));
     const double iam = rsqrt(am2);
-    const double am = am2 * iam;
-    const double un = fma(um, nx, vm * ny);
+    const double am = mul(am2, iam);
+    const double un = fma(um, nx, mul(vm, ny));
     const double eig1 = fabs(un);
     const bool sub = dlt(eig1, am);                      // |un| < am
     const double astar = sub ? am : eig1;                // (eig2 + eig3) / 2 = dmax(eig1, am)
     const double sel = sub ? un : copysign(am, un);
-    const double Mstar = sel * iam;                      // (eig2 - eig3) / (2 am)
-    const double dE = fma(UR.w, R.ir, -UL.w * L.ir);   // (HR - ER) - (HL - EL)
-    const double Etm = fma(g.Etm_c, Vm2, Hm * g.inv_gamma);
+    const double Mstar = mul(sel, iam);                  // (eig2 - eig3) / (2 am)
+    const double dE = fma(UR.w, R.ir, -mul(UL.w, L.ir));  // (HR - ER) - (HL - EL)
+    const double Etm = fma(g.Etm_c, Vm2, mul(Hm, g.inv_gamma));
     const double dW0 = R.r - L.r;
     const double du = R.u - L.u, dv = R.v - L.v;
-    const double dW1 = fma(rm, du, dW0 * um);
-    const double dW2 = fma(rm, dv, dW0 * vm);
-    const double dW3 = fma(rm, dE, dW0 * Etm);
-    const double dun = fma(nx, du, ny * dv);
+    const double dW1 = fma(rm, du, mul(dW0, um));
+    const double dW2 = fma(rm, dv, mul(dW0, vm));
+    const double dW3 = fma(rm, dE, mul(dW0, Etm));
+    const double dun = fma(nx, du, mul(ny, dv));
     const double dp = R.p - L.p;
     const double ae = astar - eig1;
-    const double dUroe = fma(Mstar, dun, ae * dp * irm * (iam * iam));
-    const double dProe = fma(Mstar, dp, ae * rm * dun);
-    const double dUr = dUroe * rm;
-    const double h = 0.5 * area;
-    F.x = h * (F.x - fma(eig1, dW0, dUr));
-    F.y = h * (F.y - fma(eig1, dW1, fma(dUr, um, dProe * nx)));
-    F.z = h * (F.z - fma(eig1, dW2, fma(dUr, vm, dProe * ny)));
-    F.w = h * (F.w - fma(eig1, dW3, fma(dUr, Hm, dProe * un)));
+    const double dUroe = fma(Mstar, dun, mul(mul(mul(ae, dp), irm), mul(iam, iam)));
+    const double dProe = fma(Mstar, dp, mul(mul(ae, rm), dun));
+    const double dUr = mul(dUroe, rm);
+    const double h = mul(0.5, area);
+    F.x = mul(h, F.x - fma(eig1, dW0, dUr));
+    F.y = mul(h, F.y - fma(eig1, dW1, fma(dUr, um, mul(dProe, nx))));
+    F.z = mul(h, F.z - fma(eig1, dW2, fma(dUr, vm, mul(dProe, ny))));
+    F.w = mul(h, F.w - fma(eig1, dW3, fma(dUr, Hm, mul(dProe, un))));
     if (REC) {
         rec->ruL = ruL; rec->ruR = ruR; rec->HL = HL; rec->HR = HR; rec->irm = irm; rec->rm = rm;
         rec->rrorl = rrorl; rec->w = w; rec->um = um; rec->vm = vm; rec->Hm = Hm; rec->am2 = am2; rec->iam = iam;
@@ -188,18 +207,18 @@ __device__ __forceinline__ d4 roe_flux(const Prim& L, const Prim& R, const d4 UL
 // (the mass flux and the total enthalpy from the conserved states, as in roe_flux)
 __device__ __forceinline__ d4 llf_flux(const d4 UL, const d4 UR, const Prim& L, const Prim& R,
                                             double nx, double ny, double length, const Gas& g) {
-    const double unL = fma(nx, L.u, ny * L.v), unR = fma(nx, R.u, ny * R.v);
-    const double ruL = fma(nx, UL.y, ny * UL.z), ruR = fma(nx, UR.y, ny * UR.z);
-    const double hl = (UL.w + L.p) * L.ir;
-    const double hr = (UR.w + R.p) * R.ir;
-    const double aL = fabs(unL) + sqrt(g.gamma * L.p * L.ir);
-    const double aR = fabs(unR) + sqrt(g.gamma * R.p * R.ir);
+    const double unL = fma(nx, L.u, mul(ny, L.v)), unR = fma(nx, R.u, mul(ny, R.v));
+    const double ruL = fma(nx, UL.y, mul(ny, UL.z)), ruR = fma(nx, UR.y, mul(ny, UR.z));
+    const double hl = mul(UL.w + L.p, L.ir);
+    const double hr = mul(UR.w + R.p, R.ir);
+    const double aL = fabs(unL) + sqrt(mul(mul(g.gamma, L.p), L.ir));
+    const double aR = fabs(unR) + sqrt(mul(mul(g.gamma, R.p), R.ir));
     const double lm = dmax(aL, aR);
-    const double hlen = 0.5 * length;
-    return mk4(hlen * (ruL + ruR - lm * (UR.x - UL.x)),
-                        hlen * (fma(ruL, L.u, nx * L.p) + fma(ruR, R.u, nx * R.p) - lm * (UR.y - UL.y)),
-                        hlen * (fma(ruL, L.v, ny * L.p) + fma(ruR, R.v, ny * R.p) - lm * (UR.z - UL.z)),
-                        hlen * (fma(ruL, hl, ruR * hr) - lm * (UR.w - UL.w)));
+    const double hlen = mul(0.5, length);
+    return mk4(mul(hlen, ruL + ruR - mul(lm, UR.x - UL.x)),
+               mul(hlen, fma(ruL, L.u, mul(nx, L.p)) + fma(ruR, R.u, mul(nx, R.p)) - mul(lm, UR.y - UL.y)),
+               mul(hlen, fma(ruL, L.v, mul(ny, L.p)) + fma(ruR, R.v, mul(ny, R.p)) - mul(lm, UR.z - UL.z)),
+               mul(hlen, fma(ruL, hl, mul(ruR, hr)) - mul(lm, UR.w - UL.w)));
 }
 
 // get_UR_wallNonViscous, FVMR/src/space/Flux.cpp:57-71

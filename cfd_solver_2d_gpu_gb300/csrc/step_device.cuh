@@ -53,14 +53,14 @@ __device__ __forceinline__ void alpha_edge(int e, const d4* __restrict__ prim, c
     d4 w = ld4(&prim[L]);
     if (R != -1) {
         const d4 wr = ld4(&prim[R]);
-        w = mk4(0.5 * (w.x + wr.x), 0.5 * (w.y + wr.y), 0.5 * (w.z + wr.z), 0.5 * (w.w + wr.w));
+        w = mk4(mul(0.5, w.x + wr.x), mul(0.5, w.y + wr.y), mul(0.5, w.z + wr.z), mul(0.5, w.w + wr.w));
     }
     if (neg(w.x) || neg(w.w)) atomicAdd(&st->negative_dt, 1ull);
     const double* gm = &m.e_geom[(size_t)e * 8];
     const double nx = __ldg(&gm[0]), ny = __ldg(&gm[1]), len = __ldg(&gm[2]), sqrt_len = __ldg(&gm[3]);
-    const double un = w.y * (nx * len) + w.z * (ny * len);
+    const double un = fma(w.y, mul(nx, len), mul(w.z, mul(ny, len)));
     const double ir = rcp(w.x);
-    alpha[e] = fabs(un) + sqrt(g.gamma * w.w * ir) * sqrt_len;
+    alpha[e] = fma(sqrt(mul(mul(g.gamma, w.w), ir)), sqrt_len, fabs(un));
     if (NS) {
         const double T = w.w / g.R * ir;
         const double mu = g.C1 * (T * sqrt(T)) * rcp(T + 110.4);
@@ -134,8 +134,8 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
 #pragma unroll
         for (int v = 0; v < 4; v++) {
             // absent neighbours carry B = 0 and dU = 0
-            gx[v] = fma(b0[2], dU[2][v], fma(b0[1], dU[1][v], b0[0] * dU[0][v]));
-            gy[v] = fma(b1[2], dU[2][v], fma(b1[1], dU[1][v], b1[0] * dU[0][v]));
+            gx[v] = fma(b0[2], dU[2][v], fma(b0[1], dU[1][v], mul(b0[0], dU[0][v])));
+            gy[v] = fma(b1[2], dU[2][v], fma(b1[1], dU[1][v], mul(b1[0], dU[0][v])));
         }
     } else {
         // GradientGreenGauss_2 (Gradient.cpp:248-458) with precomputed face weights
@@ -151,7 +151,7 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
             const double ufv[4] = {uf.x, uf.y, uf.z, uf.w};
 #pragma unroll
             for (int v = 0; v < 4; v++) {
-                const double phif = (out >= 0) ? fma(gC, ucv[v], gC1 * ufv[v]) : ucv[v];
+                const double phif = (out >= 0) ? fma(gC, ucv[v], mul(gC1, ufv[v])) : ucv[v];
                 sx[v] = fma(phif, Sx, sx[v]);
                 sy[v] = fma(phif, Sy, sy[v]);
             }
@@ -159,8 +159,8 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
         const double ginv = __ldg(&m.c_ginv[c]);
 #pragma unroll
         for (int v = 0; v < 4; v++) {
-            gx[v] = ginv * sx[v];
-            gy[v] = ginv * sy[v];
+            gx[v] = mul(ginv, sx[v]);
+            gy[v] = mul(ginv, sy[v]);
         }
     }
     static_assert(!REC || BARTH, "the adjoint's record covers the Barth limiter");
@@ -206,9 +206,9 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
                     }
                 }
             }
-            const double d0 = fma(gx[v], vx[0], gy[v] * vy[0]);
-            const double d1 = fma(gx[v], vx[1], gy[v] * vy[1]);
-            const double d2 = fma(gx[v], vx[2], gy[v] * vy[2]);
+            const double d0 = fma(gx[v], vx[0], mul(gy[v], vy[0]));
+            const double d1 = fma(gx[v], vx[1], mul(gy[v], vy[1]));
+            const double d2 = fma(gx[v], vx[2], mul(gy[v], vy[2]));
             const double dhi = dmax(dmax(d0, d1), d2), dlo = dmin(dmin(d0, d1), d2);
             int jh = 0, jl = 0;  // (REC) the vertices giving dhi / dlo, as dmax / dmin choose them
             if constexpr (REC) {
@@ -222,17 +222,17 @@ __device__ __forceinline__ void grad_cell(int c, const d4* __restrict__ U, const
             const bool lim_n = neg(dlo) && dlt(dn, nn);  // ratio nn/dn below 1
             if (lim_p || lim_n) {
                 // both limited: np/dp < nn/dn  <=>  np*dn > nn*dp  (dp > 0 > dn)
-                const bool use_p = lim_p && (!lim_n || dlt(nn * dp, np * dn));
+                const bool use_p = lim_p && (!lim_n || dlt(mul(nn, dp), mul(np, dn)));
                 const double num = use_p ? np : nn, den = use_p ? dp : dn;
                 const double rd = rcp(den);
-                const double phi = num * rd;
+                const double phi = mul(num, rd);
                 if constexpr (REC) {
                     phiv[v] = phi;
                     rdv[v] = rd;
                     code |= (1 | (((use_p ? kp : kn) + 1) << 1) | ((use_p ? jh : jl) << 3)) << (5 * v);
                 }
-                gx[v] *= phi;
-                gy[v] *= phi;
+                gx[v] = mul(gx[v], phi);
+                gy[v] = mul(gy[v], phi);
             }
         }
     }
@@ -518,7 +518,7 @@ __device__ __forceinline__ void update_cell(int c, d4* __restrict__ U, const d4*
         else { acc.x -= f.x; acc.y -= f.y; acc.z -= f.z; acc.w -= f.w; }
     }
     const double mv = __ldg(&m.c_mvol[c]);
-    const d4 k = mk4(mv * acc.x, mv * acc.y, mv * acc.z, mv * acc.w);
+    const d4 k = mk4(mul(mv, acc.x), mul(mv, acc.y), mul(mv, acc.z), mul(mv, acc.w));
     if (rec_R) rec_R[c] = k;  // the stage's residual, kept for the adjoint
     if (KIND == STAGE_RHS) {
         rhs_out[c] = k;
@@ -551,14 +551,14 @@ __device__ __forceinline__ void update_cell(int c, d4* __restrict__ U, const d4*
     } else if (KIND == STAGE_SSP_2) {
         const d4 u0 = ld4(&U0[c]);
         const d4 u = U[c];
-        un = mk4(fma(0.75, u0.x, 0.25 * fma(dt, k.x, u.x)), fma(0.75, u0.y, 0.25 * fma(dt, k.y, u.y)),
-                 fma(0.75, u0.z, 0.25 * fma(dt, k.z, u.z)), fma(0.75, u0.w, 0.25 * fma(dt, k.w, u.w)));
+        un = mk4(fma(0.75, u0.x, mul(0.25, fma(dt, k.x, u.x))), fma(0.75, u0.y, mul(0.25, fma(dt, k.y, u.y))),
+                 fma(0.75, u0.z, mul(0.25, fma(dt, k.z, u.z))), fma(0.75, u0.w, mul(0.25, fma(dt, k.w, u.w))));
     } else {  // STAGE_SSP_3
         const d4 u0 = ld4(&U0[c]);
         const d4 u = U[c];
         const double a = 1.0 / 3.0, b = 2.0 / 3.0;
-        un = mk4(fma(a, u0.x, b * fma(dt, k.x, u.x)), fma(a, u0.y, b * fma(dt, k.y, u.y)),
-                 fma(a, u0.z, b * fma(dt, k.z, u.z)), fma(a, u0.w, b * fma(dt, k.w, u.w)));
+        un = mk4(fma(a, u0.x, mul(b, fma(dt, k.x, u.x))), fma(a, u0.y, mul(b, fma(dt, k.y, u.y))),
+                 fma(a, u0.z, mul(b, fma(dt, k.z, u.z))), fma(a, u0.w, mul(b, fma(dt, k.w, u.w))));
     }
     U[c] = un;
     if (final_stage(KIND)) {

@@ -367,6 +367,22 @@ int fvgb_fp64_peak(int device, double* gflops);
  * For accuracy tests. */
 int fvgb_math_eval(int device, int n, const double* x, double* out);
 
+/* No counterpart in the reference.  The correctly rounded FP64 multiply (op 0)
+ * and add (op 1) that run on the integer pipes (softfp64.cuh) evaluated on n
+ * host pairs on the given device, beside the hardware instruction on the same
+ * pairs: soft[i] and hw[i].  For bitwise tests. */
+int fvgb_softfp64_eval(int device, int op, int n, const double* a, const double* b, double* soft, double* hw);
+/* No counterpart in the reference.  The same functions compiled for the host
+ * (the fallback is then the host's IEEE operation): out[i] = a[i] op b[i].  For
+ * CPU tests. */
+int fvgb_softfp64_host(int op, int n, const double* a, const double* b, double* out);
+/* No counterpart in the reference.  G operations/s of independent FP64 chains,
+ * eight per thread: out[0..3] multiply on the FP64 pipe alone, on the integer
+ * pipes alone, 4 + 4 and 2 + 6 side by side in one thread; out[4..7] add the
+ * same way (the last 6 + 2); out[8] the SM count, out[9] the maximum SM clock
+ * in MHz. */
+int fvgb_softfp64_rate(int device, double out[10]);
+
 const char* fvgb_last_error(void);
 const char* fvgb_version(void);
 
