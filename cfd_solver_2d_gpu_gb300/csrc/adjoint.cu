@@ -45,7 +45,7 @@ namespace fvgb {
 namespace dev {
 
 // ---- per edge --------------------------------------------------------------
-// 128-thread blocks: ~126 registers a thread leave room for four blocks per SM
+// 128-thread blocks, capped at 128 registers a thread so that four blocks fit on an SM
 constexpr int kEdgeThreads = 128;
 
 // mu = dLoss/dF_e (F_e enters R_L with +1/-vol and, when e is in R's edge list, R_R with
@@ -55,7 +55,7 @@ constexpr int kEdgeThreads = 128;
 // divided between the two sides (half each; a boundary edge's L side takes all), go to avu,
 // avgx, avgy; Uin, Gx, Gy are the stage's input state and the gradients it read.
 template <int FLUX, bool NS>
-__global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView m, Gas g, BcData bc,
+__global__ void __launch_bounds__(kEdgeThreads, 4) k_adj_edge(EdgeTape tp, MeshView m, Gas g, BcData bc,
                                                            const d4* __restrict__ lam,
                                                            const int* __restrict__ e_rlist, d4* __restrict__ aL,
                                                            d4* __restrict__ aR, const d4* __restrict__ Uin,
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kEdgeThreads) k_adj_edge(EdgeTape tp, MeshView
     const double nx = __ldg(&gm[0]), ny = __ldg(&gm[1]), len = __ldg(&gm[2]);
     const double mL = __ldg(&m.c_mvol[L]);
     const d4 lL = ld4(&lam[L]);
-    d4 mu = mk4(mL * lL.x, mL * lL.y, mL * lL.z, mL * lL.w);
+    d4 mu = mk4(mul(mL, lL.x), mul(mL, lL.y), mul(mL, lL.z), mul(mL, lL.w));
     if (__ldg(&e_rlist[e])) {
         const double mR = __ldg(&m.c_mvol[R]);
         const d4 lR = ld4(&lam[R]);
@@ -212,11 +212,11 @@ __global__ void __launch_bounds__(256) k_adj_cell(MeshView m, const d4* __restri
                 // gx_lim = phi gx, gy_lim = phi gy, phi = num / den, den = d(vertex jj) +- eps,
                 // num = U(slot kk) - Uc
                 const int kk = ((cv >> 1) & 3) - 1, jj = (cv >> 3) & 3;
-                const double b_phi = bgx * gxr[v] + bgy * gyr[v];
-                bgx *= phi[v];
-                bgy *= phi[v];
-                const double b_num = b_phi * rden[v];
-                const double b_den = -b_phi * phi[v] * rden[v];
+                const double b_phi = fma(bgy, gyr[v], mul(bgx, gxr[v]));
+                bgx = mul(bgx, phi[v]);
+                bgy = mul(bgy, phi[v]);
+                const double b_num = mul(b_phi, rden[v]);
+                const double b_den = -mul(mul(b_phi, phi[v]), rden[v]);
                 const double vxj = jj == 0 ? vx[0] : (jj == 1 ? vx[1] : vx[2]);
                 const double vyj = jj == 0 ? vy[0] : (jj == 1 ? vy[1] : vy[2]);
                 bgx = fma(b_den, vxj, bgx);
@@ -296,11 +296,11 @@ __global__ void __launch_bounds__(256) k_adj_combine(MeshView m, const int* __re
         const double dt = *dt_p;
         const d4 ls = ld4(&lam_s[c]);
         const d4 rs = ld4(&R_s[c]);
-        dot = fma(ls.x, rs.x, fma(ls.y, rs.y, fma(ls.z, rs.z, ls.w * rs.w)));
-        d4 li = mk4(b * fma(dt, r[0], ci * ls.x), b * fma(dt, r[1], ci * ls.y), b * fma(dt, r[2], ci * ls.z),
-                    b * fma(dt, r[3], ci * ls.w));
+        dot = fma(ls.x, rs.x, fma(ls.y, rs.y, fma(ls.z, rs.z, mul(ls.w, rs.w))));
+        d4 li = mk4(mul(b, fma(dt, r[0], mul(ci, ls.x))), mul(b, fma(dt, r[1], mul(ci, ls.y))),
+                    mul(b, fma(dt, r[2], mul(ci, ls.z))), mul(b, fma(dt, r[3], mul(ci, ls.w))));
         if (acc_mode == 0) {
-            acc0[c] = mk4(a * ls.x, a * ls.y, a * ls.z, a * ls.w);
+            acc0[c] = mk4(mul(a, ls.x), mul(a, ls.y), mul(a, ls.z), mul(a, ls.w));
         } else if (acc_mode == 1) {
             const d4 o = acc0[c];
             acc0[c] = mk4(fma(a, ls.x, o.x), fma(a, ls.y, o.y), fma(a, ls.z, o.z), fma(a, ls.w, o.w));

@@ -14,17 +14,17 @@ __device__ __forceinline__ double sgn(double x) { return pos(x) ? 1.0 : (neg(x) 
 
 // adjoint of to_prim: (bw.r, bw.u, bw.v, bw.p, bw.ir) -> dL/dU added to bU
 __device__ __forceinline__ void to_prim_vjp(const d4 U, const Prim& w, const Gas& g, const Prim& bw, d4& bU) {
-    const double q = U.w * w.ir - 0.5 * (w.u * w.u + w.v * w.v);
-    const double b_q = bw.p * w.r * g.ga1;
-    double b_ir = bw.ir + b_q * U.w;
-    const double b_u = bw.u - b_q * w.u;
-    const double b_v = bw.v - b_q * w.v;
-    bU.w += b_q * w.ir;
-    bU.y += b_u * w.ir;
-    b_ir += b_u * U.y;
-    bU.z += b_v * w.ir;
-    b_ir += b_v * U.z;
-    bU.x += bw.r + bw.p * g.ga1 * q - b_ir * w.ir * w.ir;
+    const double q = fma(-0.5, fma(w.u, w.u, mul(w.v, w.v)), mul(U.w, w.ir));
+    const double b_q = mul(mul(bw.p, w.r), g.ga1);
+    double b_ir = fma(b_q, U.w, bw.ir);
+    const double b_u = fma(-b_q, w.u, bw.u);
+    const double b_v = fma(-b_q, w.v, bw.v);
+    bU.w = fma(b_q, w.ir, bU.w);
+    bU.y = fma(b_u, w.ir, bU.y);
+    b_ir = fma(b_u, U.y, b_ir);
+    bU.z = fma(b_v, w.ir, bU.z);
+    b_ir = fma(b_v, U.z, b_ir);
+    bU.x += fma(-mul(b_ir, w.ir), w.ir, fma(mul(bw.p, g.ga1), q, bw.r));
 }
 
 // adjoint of roe_flux (physics.cuh): bF -> adjoints of the two primitive states (bL, bR,
@@ -41,74 +41,74 @@ __device__ __forceinline__ void roe_rev(const Prim& L, const Prim& R, const d4 U
     const double Mstar = r.Mstar, dE = r.dE, Etm = r.Etm, ae = r.ae, dUroe = r.dUroe, dProe = r.dProe, dUr = r.dUr;
     const bool sub = r.sub;
     const double sL = UL.w + L.p, sR = UR.w + R.p;
-    const double prod = R.r * L.r;
+    const double prod = mul(R.r, L.r);
     const double Xu = fma(R.u, rrorl, L.u), Xv = fma(R.v, rrorl, L.v), XH = fma(HR, rrorl, HL);
     const double eig1 = fabs(un);
     const double dW0 = R.r - L.r;
     const double du = R.u - L.u, dv = R.v - L.v;
-    const double dW1 = fma(rm, du, dW0 * um);
-    const double dW2 = fma(rm, dv, dW0 * vm);
-    const double dW3 = fma(rm, dE, dW0 * Etm);
-    const double dun = fma(nx, du, ny * dv);
+    const double dW1 = fma(rm, du, mul(dW0, um));
+    const double dW2 = fma(rm, dv, mul(dW0, vm));
+    const double dW3 = fma(rm, dE, mul(dW0, Etm));
+    const double dun = fma(nx, du, mul(ny, dv));
     const double dp = R.p - L.p;
-    const double iam2 = iam * iam;
-    const double t1 = ae * dp, t12 = t1 * irm;   // dUroe's second term is t12 iam2
-    const double t3 = ae * rm;                   // dProe's second term is t3 dun
-    const double h = 0.5 * area;
+    const double iam2 = mul(iam, iam);
+    const double t1 = mul(ae, dp), t12 = mul(t1, irm);  // dUroe's second term is t12 iam2
+    const double t3 = mul(ae, rm);                      // dProe's second term is t3 dun
+    const double h = mul(0.5, area);
     // ---- reverse ----
-    const double bC0 = h * bF.x, bC1 = h * bF.y, bC2 = h * bF.z, bC3 = h * bF.w;  // central part
-    const double bD0 = -bC0, bD1 = -bC1, bD2 = -bC2, bD3 = -bC3;                   // dissipation
-    double b_eig1 = bD0 * dW0 + bD1 * dW1 + bD2 * dW2 + bD3 * dW3;
-    double b_dW0 = bD0 * eig1;
-    const double b_dW1 = bD1 * eig1, b_dW2 = bD2 * eig1, b_dW3 = bD3 * eig1;
-    const double b_dUr = bD0 + bD1 * um + bD2 * vm + bD3 * Hm;
-    double b_um = bD1 * dUr, b_vm = bD2 * dUr, b_Hm = bD3 * dUr;
-    const double b_dProe = bD1 * nx + bD2 * ny + bD3 * un;
-    double b_un = bD3 * dProe;
+    const double bC0 = mul(h, bF.x), bC1 = mul(h, bF.y), bC2 = mul(h, bF.z), bC3 = mul(h, bF.w);  // central part
+    const double bD0 = -bC0, bD1 = -bC1, bD2 = -bC2, bD3 = -bC3;                                    // dissipation
+    double b_eig1 = fma(bD3, dW3, fma(bD2, dW2, fma(bD1, dW1, mul(bD0, dW0))));
+    double b_dW0 = mul(bD0, eig1);
+    const double b_dW1 = mul(bD1, eig1), b_dW2 = mul(bD2, eig1), b_dW3 = mul(bD3, eig1);
+    const double b_dUr = fma(bD3, Hm, fma(bD2, vm, fma(bD1, um, bD0)));
+    double b_um = mul(bD1, dUr), b_vm = mul(bD2, dUr), b_Hm = mul(bD3, dUr);
+    const double b_dProe = fma(bD3, un, fma(bD2, ny, mul(bD1, nx)));
+    double b_un = mul(bD3, dProe);
     // dUr = dUroe rm
-    const double b_dUroe = b_dUr * rm;
-    double b_rm = b_dUr * dUroe;
+    const double b_dUroe = mul(b_dUr, rm);
+    double b_rm = mul(b_dUr, dUroe);
     // dProe = Mstar dp + t3 dun
-    double b_Mstar = b_dProe * dp;
-    double b_dp = b_dProe * Mstar;
-    const double b_t3 = b_dProe * dun;
-    double b_dun = b_dProe * t3;
-    double b_ae = b_t3 * rm;
-    b_rm += b_t3 * ae;
+    double b_Mstar = mul(b_dProe, dp);
+    double b_dp = mul(b_dProe, Mstar);
+    const double b_t3 = mul(b_dProe, dun);
+    double b_dun = mul(b_dProe, t3);
+    double b_ae = mul(b_t3, rm);
+    b_rm = fma(b_t3, ae, b_rm);
     // dUroe = Mstar dun + t12 iam2
-    b_Mstar += b_dUroe * dun;
-    b_dun += b_dUroe * Mstar;
-    const double b_iam2 = b_dUroe * t12;
-    const double b_t12 = b_dUroe * iam2;
-    double b_irm = b_t12 * t1;
-    const double b_t1 = b_t12 * irm;
-    b_ae += b_t1 * dp;
-    b_dp += b_t1 * ae;
-    double b_iam = 2.0 * iam * b_iam2;
+    b_Mstar = fma(b_dUroe, dun, b_Mstar);
+    b_dun = fma(b_dUroe, Mstar, b_dun);
+    const double b_iam2 = mul(b_dUroe, t12);
+    const double b_t12 = mul(b_dUroe, iam2);
+    double b_irm = mul(b_t12, t1);
+    const double b_t1 = mul(b_t12, irm);
+    b_ae = fma(b_t1, dp, b_ae);
+    b_dp = fma(b_t1, ae, b_dp);
+    double b_iam = mul(mul(2.0, iam), b_iam2);
     // ae = astar - eig1; astar = am or eig1
     double b_am = sub ? b_ae : 0.0;
     b_eig1 += sub ? -b_ae : 0.0;  // astar = eig1 when not sub: the two cancel
     // dp, dun, dW*, dE, Etm
     double b_Rp = b_dp, b_Lp = -b_dp;
-    double b_du = b_dun * nx, b_dv = b_dun * ny;
-    b_rm += b_dW3 * dE + b_dW2 * dv + b_dW1 * du;
-    const double b_dE = b_dW3 * rm;
-    const double b_Etm = b_dW3 * dW0;
-    b_dW0 += b_dW3 * Etm + b_dW2 * vm + b_dW1 * um;
-    b_dv += b_dW2 * rm;
-    b_vm += b_dW2 * dW0;
-    b_du += b_dW1 * rm;
-    b_um += b_dW1 * dW0;
+    double b_du = mul(b_dun, nx), b_dv = mul(b_dun, ny);
+    b_rm += fma(b_dW1, du, fma(b_dW2, dv, mul(b_dW3, dE)));
+    const double b_dE = mul(b_dW3, rm);
+    const double b_Etm = mul(b_dW3, dW0);
+    b_dW0 += fma(b_dW1, um, fma(b_dW2, vm, mul(b_dW3, Etm)));
+    b_dv = fma(b_dW2, rm, b_dv);
+    b_vm = fma(b_dW2, dW0, b_vm);
+    b_du = fma(b_dW1, rm, b_du);
+    b_um = fma(b_dW1, dW0, b_um);
     double b_Rr = b_dW0, b_Lr = -b_dW0;
     double b_Ru = b_du, b_Lu = -b_du, b_Rv = b_dv, b_Lv = -b_dv;
-    double b_Vm2 = b_Etm * g.Etm_c;
-    b_Hm += b_Etm * g.inv_gamma;
+    double b_Vm2 = mul(b_Etm, g.Etm_c);
+    b_Hm = fma(b_Etm, g.inv_gamma, b_Hm);
     // dE = URw Rir - ULw Lir
-    double b_URw = b_dE * R.ir, b_ULw = -b_dE * L.ir;
-    double b_Rir = b_dE * UR.w, b_Lir = -b_dE * UL.w;
+    double b_URw = mul(b_dE, R.ir), b_ULw = -mul(b_dE, L.ir);
+    double b_Rir = mul(b_dE, UR.w), b_Lir = -mul(b_dE, UL.w);
     // Mstar = sel iam; sel = un (sub) or copysign(am, un)
-    const double b_sel = b_Mstar * iam;
-    b_iam += b_Mstar * sel;
+    const double b_sel = mul(b_Mstar, iam);
+    b_iam = fma(b_Mstar, sel, b_iam);
     if (sub) b_un += b_sel;
     else b_am += b_sel * copysign(1.0, un);
     // eig1 = |un|; un = um nx + vm ny
@@ -116,54 +116,54 @@ __device__ __forceinline__ void roe_rev(const Prim& L, const Prim& R, const d4 U
     b_um += b_un * nx;
     b_vm += b_un * ny;
     // am = am2 iam; iam = am2^(-1/2); am2 = ga1 (Hm - Vm2/2); Vm2 = um^2 + vm^2
-    double b_am2 = b_am * iam;
-    b_iam += b_am * am2;
-    b_am2 -= 0.5 * b_iam * iam * iam2;
-    b_Hm += b_am2 * g.ga1;
-    b_Vm2 -= 0.5 * g.ga1 * b_am2;
-    b_um += 2.0 * um * b_Vm2;
-    b_vm += 2.0 * vm * b_Vm2;
+    double b_am2 = mul(b_am, iam);
+    b_iam = fma(b_am, am2, b_iam);
+    b_am2 = fma(-mul(mul(0.5, b_iam), iam), iam2, b_am2);
+    b_Hm = fma(b_am2, g.ga1, b_Hm);
+    b_Vm2 = fma(-mul(0.5, g.ga1), b_am2, b_Vm2);
+    b_um = fma(mul(2.0, um), b_Vm2, b_um);
+    b_vm = fma(mul(2.0, vm), b_Vm2, b_vm);
     // (um, vm, Hm) = (Xu, Xv, XH) w
-    const double b_w = b_um * Xu + b_vm * Xv + b_Hm * XH;
-    const double bXu = b_um * w, bXv = b_vm * w, bXH = b_Hm * w;
-    b_Ru += bXu * rrorl;
+    const double b_w = fma(b_Hm, XH, fma(b_vm, Xv, mul(b_um, Xu)));
+    const double bXu = mul(b_um, w), bXv = mul(b_vm, w), bXH = mul(b_Hm, w);
+    b_Ru = fma(bXu, rrorl, b_Ru);
     b_Lu += bXu;
-    b_Rv += bXv * rrorl;
+    b_Rv = fma(bXv, rrorl, b_Rv);
     b_Lv += bXv;
-    double b_HR = bXH * rrorl, b_HL = bXH;
-    double b_rrorl = bXu * R.u + bXv * R.v + bXH * HR - b_w * w * w;
+    double b_HR = mul(bXH, rrorl), b_HL = bXH;
+    double b_rrorl = fma(-mul(b_w, w), w, fma(bXH, HR, fma(bXv, R.v, mul(bXu, R.u))));
     // rrorl = Rr irm; rm = prod irm; irm = prod^(-1/2); prod = Rr Lr
-    b_Rr += b_rrorl * irm;
-    b_irm += b_rrorl * R.r;
-    double b_prod = b_rm * irm;
-    b_irm += b_rm * prod;
-    b_prod -= 0.5 * b_irm * irm * irm * irm;
-    b_Rr += b_prod * L.r;
-    b_Lr += b_prod * R.r;
+    b_Rr = fma(b_rrorl, irm, b_Rr);
+    b_irm = fma(b_rrorl, R.r, b_irm);
+    double b_prod = mul(b_rm, irm);
+    b_irm = fma(b_rm, prod, b_irm);
+    b_prod = fma(-mul(mul(mul(0.5, b_irm), irm), irm), irm, b_prod);
+    b_Rr = fma(b_prod, L.r, b_Rr);
+    b_Lr = fma(b_prod, R.r, b_Lr);
     // central flux (ruL + ruR, ruL uL + ruR uR + nx psum, ruL vL + ruR vR + ny psum, ruL HL + ruR HR)
-    const double b_ruL = bC0 + bC1 * L.u + bC2 * L.v + bC3 * HL;
-    const double b_ruR = bC0 + bC1 * R.u + bC2 * R.v + bC3 * HR;
-    b_Lu += bC1 * ruL;
-    b_Ru += bC1 * ruR;
-    b_Lv += bC2 * ruL;
-    b_Rv += bC2 * ruR;
-    b_HL += bC3 * ruL;
-    b_HR += bC3 * ruR;
-    const double b_psum = bC1 * nx + bC2 * ny;
+    const double b_ruL = fma(bC3, HL, fma(bC2, L.v, fma(bC1, L.u, bC0)));
+    const double b_ruR = fma(bC3, HR, fma(bC2, R.v, fma(bC1, R.u, bC0)));
+    b_Lu = fma(bC1, ruL, b_Lu);
+    b_Ru = fma(bC1, ruR, b_Ru);
+    b_Lv = fma(bC2, ruL, b_Lv);
+    b_Rv = fma(bC2, ruR, b_Rv);
+    b_HL = fma(bC3, ruL, b_HL);
+    b_HR = fma(bC3, ruR, b_HR);
+    const double b_psum = fma(bC2, ny, mul(bC1, nx));
     b_Lp += b_psum;
     b_Rp += b_psum;
     // H = (rho E + p) / rho
-    b_ULw += b_HL * L.ir;
-    b_Lp += b_HL * L.ir;
-    b_Lir += b_HL * sL;
-    b_URw += b_HR * R.ir;
-    b_Rp += b_HR * R.ir;
-    b_Rir += b_HR * sR;
+    b_ULw = fma(b_HL, L.ir, b_ULw);
+    b_Lp = fma(b_HL, L.ir, b_Lp);
+    b_Lir = fma(b_HL, sL, b_Lir);
+    b_URw = fma(b_HR, R.ir, b_URw);
+    b_Rp = fma(b_HR, R.ir, b_Rp);
+    b_Rir = fma(b_HR, sR, b_Rir);
     bL.r = b_Lr; bL.u = b_Lu; bL.v = b_Lv; bL.p = b_Lp; bL.ir = b_Lir;
     bR.r = b_Rr; bR.u = b_Ru; bR.v = b_Rv; bR.p = b_Rp; bR.ir = b_Rir;
     // mass fluxes n . (rho u)
-    bUL = mk4(0.0, b_ruL * nx, b_ruL * ny, b_ULw);
-    bUR = mk4(0.0, b_ruR * nx, b_ruR * ny, b_URw);
+    bUL = mk4(0.0, mul(b_ruL, nx), mul(b_ruL, ny), b_ULw);
+    bUR = mk4(0.0, mul(b_ruR, nx), mul(b_ruR, ny), b_URw);
 }
 
 // the same with the forward recomputed (for a caller without the recorded intermediates)
