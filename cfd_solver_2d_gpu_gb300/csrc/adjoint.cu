@@ -360,95 +360,106 @@ __global__ void __launch_bounds__(kDtThreads) k_adj_dt(const double* __restrict_
                                                        double b0, double b1, double b2, const d4* __restrict__ U0,
                                                        MeshView m, Gas g, double CFL, const int* cstar,
                                                        const double* dt_info, d4* lam, int ns, double value_1) {
-    __shared__ double red[kDtThreads];
-    double lt = 0.0;
+    // lt = sum over the stages of b_s (sum of the stage's block partials): each thread sums its
+    // share of every stage, then the warps and the block reduce in a fixed order
+    __shared__ double red[kDtThreads / 32];
+    double x = 0.0;
     for (int st = 0; st < nstages; st++) {
-        double x = 0.0;
-        for (int i = threadIdx.x; i < nb; i += kDtThreads) x += part[(size_t)st * nb + i];
-        red[threadIdx.x] = x;
-        __syncthreads();
-        for (int w = kDtThreads / 2; w > 0; w >>= 1) {
-            if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-            __syncthreads();
-        }
-        lt = fma(st == 0 ? b0 : (st == 1 ? b1 : b2), red[0], lt);
-        __syncthreads();
+        const double bs = st == 0 ? b0 : (st == 1 ? b1 : b2);
+        double y = 0.0;
+        for (int i = threadIdx.x; i < nb; i += kDtThreads) y += part[(size_t)st * nb + i];
+        x = fma(bs, y, x);
     }
-    if (threadIdx.x != 0) return;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    double lt = 0.0;
+    for (int i = 0; i < kDtThreads / 32; i++) lt += red[i];
     const int c = *cstar;
     if (c < 0 || c >= m.N) return;
     if (dt_info[0] != dt_info[1]) return;  // clamped to the end time: dt does not depend on U
     if (lt == 0.0) return;
-    double alpha = 0.0;
-    for (int k = m.dt_ptr[c]; k < m.dt_ptr[c + 1]; k++) {
-        const int e = m.dt_edge[k];
-        const int L = m.e_L[e], R = m.e_R[e];
-        const Prim wl = to_prim(U0[L], g);
-        d4 w = mk4(wl.r, wl.u, wl.v, wl.p);
+    // d dt / d U at the argmin cell: dt = CFL vol / alpha, alpha = the cell's sum over its edges
+    // (k_alpha, dt_cell); one lane per edge, the sums and the updates of lam in the edge order
+    const int k0 = m.dt_ptr[c], ne = m.dt_ptr[c + 1] - k0;
+    if (ne > 32) return;  // a cell has at most four edge slots
+    const bool act = lane < ne;
+    const int e = act ? m.dt_edge[k0 + lane] : 0;
+    const int L = act ? m.e_L[e] : 0, R = act ? m.e_R[e] : -1;
+    Prim wl{}, wr{};
+    d4 w = mk4(0, 0, 0, 0);
+    double term = 0.0, nxl = 0.0, nyl = 0.0, ir = 0.0, sq = 0.0, un = 0.0, gm2 = 0.0, gm3 = 0.0;
+    if (act) {
+        wl = to_prim(U0[L], g);
+        w = mk4(wl.r, wl.u, wl.v, wl.p);
         if (R != -1) {
-            const Prim wr = to_prim(U0[R], g);
-            w = mk4(0.5 * (w.x + wr.r), 0.5 * (w.y + wr.u), 0.5 * (w.z + wr.v), 0.5 * (w.w + wr.p));
+            wr = to_prim(U0[R], g);
+            w = mk4(mul(0.5, w.x + wr.r), mul(0.5, w.y + wr.u), mul(0.5, w.z + wr.v), mul(0.5, w.w + wr.p));
         }
         const double* gm = &m.e_geom[(size_t)e * 8];
-        const double un = w.y * (gm[0] * gm[2]) + w.z * (gm[1] * gm[2]);
-        alpha += fabs(un) + sqrt(g.gamma * w.w * rcp(w.x)) * gm[3];
+        gm2 = gm[2];
+        gm3 = gm[3];
+        nxl = mul(gm[0], gm2);
+        nyl = mul(gm[1], gm2);
+        un = fma(w.y, nxl, mul(w.z, nyl));
+        ir = rcp(w.x);
+        sq = sqrt(mul(mul(g.gamma, w.w), ir));
+        term = fma(sq, gm3, fabs(un));
         if (ns) {  // the viscous spectral radius (k_alpha<true>, dt_cell<true>)
-            const double ir = rcp(w.x);
-            const double T = w.w / g.R * ir;
-            const double mu = g.C1 * (T * sqrt(T)) * rcp(T + 110.4);
-            alpha = fma(2.0 * gm[2] * value_1 * mu * ir, rcp(m.c_vol[c]), alpha);
+            const double T = mul(w.w / g.R, ir);
+            const double mu = mul(mul(g.C1, mul(T, sqrt(T))), rcp(T + 110.4));
+            term = mul(mul(mul(mul(2.0, gm2), value_1), mu), ir);  // alpha_vis; scaled by 1/vol below
         }
     }
     const double vol = m.c_vol[c];
-    const double dt = CFL * vol * rcp(alpha);
-    const double b_alpha = lt * (-dt * rcp(alpha));
-    for (int k = m.dt_ptr[c]; k < m.dt_ptr[c + 1]; k++) {
-        const int e = m.dt_edge[k];
-        const int L = m.e_L[e], R = m.e_R[e];
-        const Prim wl = to_prim(U0[L], g);
-        Prim wr{};
-        d4 w = mk4(wl.r, wl.u, wl.v, wl.p);
-        if (R != -1) {
-            wr = to_prim(U0[R], g);
-            w = mk4(0.5 * (w.x + wr.r), 0.5 * (w.y + wr.u), 0.5 * (w.z + wr.v), 0.5 * (w.w + wr.p));
-        }
-        const double* gm = &m.e_geom[(size_t)e * 8];
-        const double nxl = gm[0] * gm[2], nyl = gm[1] * gm[2];
-        const double un = w.y * nxl + w.z * nyl;
-        const double ir = rcp(w.x);
-        const double s = sqrt(g.gamma * w.w * ir);
-        const double b_un = b_alpha * sgn(un);
-        const double b_s = b_alpha * gm[3];
-        const double b_p = s > 0 ? b_s * g.gamma * ir / (2.0 * s) : 0.0;
-        const double b_ir = s > 0 ? b_s * g.gamma * w.w / (2.0 * s) : 0.0;
+    double alpha = 0.0;
+    for (int k = 0; k < ne; k++) {  // the cell's sum in the edge order, as dt_cell forms it
+        const double tk = __shfl_sync(0xffffffffu, term, k);
+        const double sk = ns ? __shfl_sync(0xffffffffu, fma(sq, gm3, fabs(un)), k) : tk;
+        alpha += sk;
+        if (ns) alpha = fma(tk, rcp(vol), alpha);
+    }
+    const double dt = mul(mul(CFL, vol), rcp(alpha));
+    const double b_alpha = mul(lt, -mul(dt, rcp(alpha)));
+    d4 buL = mk4(0, 0, 0, 0), buR = mk4(0, 0, 0, 0);
+    if (act) {
+        const double b_un = mul(b_alpha, sgn(un));
+        const double b_s = mul(b_alpha, gm3);
+        const double b_p = sq > 0 ? mul(mul(b_s, g.gamma), ir) / (2.0 * sq) : 0.0;
+        const double b_ir = sq > 0 ? mul(mul(b_s, g.gamma), w.w) / (2.0 * sq) : 0.0;
         Prim bw{};
-        bw.r = -b_ir * ir * ir;
-        bw.u = b_un * nxl;
-        bw.v = b_un * nyl;
+        bw.r = -mul(mul(b_ir, ir), ir);
+        bw.u = mul(b_un, nxl);
+        bw.v = mul(b_un, nyl);
         bw.p = b_p;
         if (ns) {  // alpha_vis = 2 L value_1 mu(T) / rho / vol, T = p / (R rho)
-            const double T = w.w / g.R * ir;
-            const double mu = g.C1 * (T * sqrt(T)) * rcp(T + 110.4);
-            const double b_av = b_alpha * rcp(vol);
-            const double k = 2.0 * gm[2] * value_1;
-            const double b_mu = b_av * k * ir;
-            const double b_T = b_mu * mu * (1.5 / T - 1.0 / (T + 110.4));
-            const double b_irv = b_av * k * mu + b_T * w.w / g.R;
-            bw.r -= b_irv * ir * ir;
-            bw.p += b_T * ir / g.R;
+            const double T = mul(w.w / g.R, ir);
+            const double mu = mul(mul(g.C1, mul(T, sqrt(T))), rcp(T + 110.4));
+            const double b_av = mul(b_alpha, rcp(vol));
+            const double kk = mul(mul(2.0, gm2), value_1);
+            const double b_mu = mul(mul(b_av, kk), ir);
+            const double b_T = mul(mul(b_mu, mu), 1.5 / T - 1.0 / (T + 110.4));
+            const double b_irv = fma(mul(b_av, kk), mu, mul(b_T, w.w) / g.R);
+            bw.r = fma(-mul(b_irv, ir), ir, bw.r);
+            bw.p = fma(b_T, ir / g.R, bw.p);
         }
         const double f = (R != -1) ? 0.5 : 1.0;
-        Prim bc{f * bw.r, f * bw.u, f * bw.v, f * bw.p, 0.0};
-        d4 bu = mk4(0, 0, 0, 0);
-        to_prim_vjp(U0[L], wl, g, bc, bu);
-        d4 o = lam[L];
-        lam[L] = mk4(o.x + bu.x, o.y + bu.y, o.z + bu.z, o.w + bu.w);
-        if (R != -1) {
-            bu = mk4(0, 0, 0, 0);
-            to_prim_vjp(U0[R], wr, g, bc, bu);
-            o = lam[R];
-            lam[R] = mk4(o.x + bu.x, o.y + bu.y, o.z + bu.z, o.w + bu.w);
+        const Prim bc{mul(f, bw.r), mul(f, bw.u), mul(f, bw.v), mul(f, bw.p), 0.0};
+        to_prim_vjp(U0[L], wl, g, bc, buL);
+        if (R != -1) to_prim_vjp(U0[R], wr, g, bc, buR);
+    }
+    for (int k = 0; k < ne; k++) {  // the updates of lam in the edge order (edges share cells)
+        if (lane == k) {
+            d4 o = lam[L];
+            lam[L] = mk4(o.x + buL.x, o.y + buL.y, o.z + buL.z, o.w + buL.w);
+            if (R != -1) {
+                o = lam[R];
+                lam[R] = mk4(o.x + buR.x, o.y + buR.y, o.z + buR.z, o.w + buR.w);
+            }
         }
+        __syncwarp();
     }
 }
 

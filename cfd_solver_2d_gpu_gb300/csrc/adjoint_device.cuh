@@ -37,7 +37,7 @@ __device__ __forceinline__ void roe_rev(const Prim& L, const Prim& R, const d4 U
                                         double area, const Gas& g, const RoeRec& r, const d4 bF, Prim& bL, Prim& bR,
                                         d4& bUL, d4& bUR) {
     const double ruL = r.ruL, ruR = r.ruR, HL = r.HL, HR = r.HR, irm = r.irm, rm = r.rm, rrorl = r.rrorl, w = r.w;
-    const double um = r.um, vm = r.vm, Hm = r.Hm, am2 = r.am2, iam = r.iam, am = r.am, un = r.un, sel = r.sel;
+    const double um = r.um, vm = r.vm, Hm = r.Hm, am2 = r.am2, iam = r.iam, un = r.un, sel = r.sel;
     const double Mstar = r.Mstar, dE = r.dE, Etm = r.Etm, ae = r.ae, dUroe = r.dUroe, dProe = r.dProe, dUr = r.dUr;
     const bool sub = r.sub;
     const double sL = UL.w + L.p, sR = UR.w + R.p;
