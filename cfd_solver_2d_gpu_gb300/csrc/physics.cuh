@@ -4,7 +4,7 @@
 // formulas are rearranged to spend fewer FP64 divides and square roots (the
 // FP64 pipe, not HBM, bounds this step on GB300): one reciprocal of rho per
 // state instead of three divides, one reciprocal square root for the Roe
-// average, T*sqrt(T) for T^1.5.  Results differ from the reference's by a few
+// average, T*sqrt(T) for T^1.5, square roots from the reciprocal square root.  Results differ from the reference's by a few
 // ulp per operation; decisions (range checks, limiter bounds, far-field
 // branches) are taken on the same quantities in the same way.
 #pragma once
@@ -94,6 +94,28 @@ __device__ __forceinline__ double rcp(double x) {
     return fma(y, fma(e, e, e), y);
 }
 
+// 1/sqrt(x) and sqrt(x) for normal x > 0: the hardware's approximate reciprocal square root
+// y (relative error below 2^-22) refined by the series (1 - e)^(-1/2) = 1 + e/2 + 3e^2/8 +
+// O(e^3), e = 1 - x y^2, whose truncation is below 2^-63; sqrt(x) = x rsq(x).  Both are
+// within ~1.5 ulp of the correctly rounded value.  Zero, subnormal, negative, infinite and
+// NaN arguments call the library functions out of line (a real branch: see softfp64.cuh).
+static __device__ __noinline__ double rsq_rare(double x) { return rsqrt(x); }
+static __device__ __noinline__ double sq_rare(double x) { return sqrt(x); }
+__device__ __forceinline__ bool normal_pos(double x) {
+    return (unsigned long long)__double_as_longlong(x) - 0x0010000000000000ull < 0x7fe0000000000000ull;
+}
+__device__ __forceinline__ double rsq(double x) {
+    if (!normal_pos(x)) return rsq_rare(x);
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double e = fma(-x, mul(y, y), 1.0);
+    return fma(mul(y, e), fma(0.375, e, 0.5), y);
+}
+__device__ __forceinline__ double sq(double x) {
+    if (!normal_pos(x)) return sq_rare(x);
+    return mul(x, rsq(x));
+}
+
 // U2ruvp_host, FVMR/src/math/PhysicalKernel.h:11-18; the pressure as
 // (gamma-1) (rho E - (rho u u + rho v v)/2), equal to the reference's
 // rho (gamma-1) (E/rho - (u u + v v)/2) with four FP64 operations instead of six
@@ -154,7 +176,7 @@ __device__ __forceinline__ d4 roe_core(const Prim& L, const Prim& R, const d4 UL
                fma(ruL, HL, mul(ruR, HR)));
     // Roe averages: rm = sqrt(rR rL), rrorl = sqrt(rR/rL) = rR / rm
     const double prod = mul(R.r, L.r);
-    const double irm = rsqrt(prod);
+    const double irm = rsq(prod);
     const double rm = mul(prod, irm);
     const double rrorl = mul(R.r, irm);
     const double w = rcp(rrorl + 1.0);
@@ -163,7 +185,7 @@ __device__ __forceinline__ d4 roe_core(const Prim& L, const Prim& R, const d4 UL
     const double Hm = mul(fma(HR, rrorl, HL), w);
     const double Vm2 = fma(um, um, mul(vm, vm));
     const double am2 = mul(g.ga1, fma(-0.5, Vm2, Hm));
-    const double iam = rsqrt(am2);
+    const double iam = rsq(am2);
     const double am = mul(am2, iam);
     const double un = fma(um, nx, mul(vm, ny));
     const double eig1 = fabs(un);
@@ -211,8 +233,8 @@ __device__ __forceinline__ d4 llf_flux(const d4 UL, const d4 UR, const Prim& L, 
     const double ruL = fma(nx, UL.y, mul(ny, UL.z)), ruR = fma(nx, UR.y, mul(ny, UR.z));
     const double hl = mul(UL.w + L.p, L.ir);
     const double hr = mul(UR.w + R.p, R.ir);
-    const double aL = fabs(unL) + sqrt(mul(mul(g.gamma, L.p), L.ir));
-    const double aR = fabs(unR) + sqrt(mul(mul(g.gamma, R.p), R.ir));
+    const double aL = fabs(unL) + sq(mul(mul(g.gamma, L.p), L.ir));
+    const double aR = fabs(unR) + sq(mul(mul(g.gamma, R.p), R.ir));
     const double lm = dmax(aL, aR);
     const double hlen = mul(0.5, length);
     return mk4(mul(hlen, ruL + ruR - mul(lm, UR.x - UL.x)),
@@ -283,7 +305,7 @@ __device__ __forceinline__ void viscous_flux(d4& F, const d4 U, const d4 gx, con
     const double T = g.inv_Cv * (E - 0.5 * (u * u + v * v));
     const double dTdx = (dEdx - u * dudx - v * dvdx) * g.inv_Cv;
     const double dTdy = (dEdy - u * dudy - v * dvdy) * g.inv_Cv;
-    const double mu = g.C1 * (T * sqrt(T)) * rcp(T + 110.4);
+    const double mu = mul(mul(g.C1, mul(T, sq(T))), rcp(T + 110.4));
     const double div = dudx + dvdy;
     const double NMD = -2.0 / 3.0;
     const double txx = mu * fma(NMD, div, 2.0 * dudx);

@@ -31,10 +31,10 @@ __global__ void __launch_bounds__(kThreads) k_fma_chain(double* __restrict__ out
     out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
-// the library's reciprocal on n values
-__global__ void k_math_eval(const double* __restrict__ x, double* __restrict__ out, int n) {
+// the library's reciprocal (op 0), reciprocal square root (1) or square root (2) on n values
+__global__ void k_math_eval(int op, const double* __restrict__ x, double* __restrict__ out, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = fvgb::dev::rcp(x[i]);
+    if (i < n) out[i] = op == 0 ? fvgb::dev::rcp(x[i]) : (op == 1 ? fvgb::dev::rsq(x[i]) : fvgb::dev::sq(x[i]));
 }
 
 // Throughput of correctly rounded FP64 multiply (OP 0) or add (OP 1): HW independent chains
@@ -130,17 +130,19 @@ extern "C" int fvgb_fp64_peak(int device, double* gflops) {
     return 0;
 }
 
-// No counterpart in the reference: the device reciprocal rcp (physics.cuh) evaluated on
-// n host values, for accuracy tests against correctly rounded results.
-extern "C" int fvgb_math_eval(int device, int n, const double* x, double* out) {
-    if (n < 0 || (n > 0 && (!x || !out))) return fvgb::fail(FVGB_ERR_ARG, "fvgb_math_eval: bad arguments");
+// No counterpart in the reference: the device reciprocal rcp, reciprocal square root rsq or
+// square root sq (physics.cuh; op 0, 1, 2) evaluated on n host values, for accuracy tests
+// against correctly rounded results.
+extern "C" int fvgb_math_eval(int device, int op, int n, const double* x, double* out) {
+    if (n < 0 || op < 0 || op > 2 || (n > 0 && (!x || !out)))
+        return fvgb::fail(FVGB_ERR_ARG, "fvgb_math_eval: bad arguments");
     if (n == 0) return 0;
     double* buf = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     PK(cudaSetDevice(device));
     PK(cudaMalloc(&buf, sizeof(double) * 2 * (size_t)n));
     PK(cudaMemcpy(buf, x, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice));
-    k_math_eval<<<(n + 255) / 256, 256>>>(buf, buf + n, n);
+    k_math_eval<<<(n + 255) / 256, 256>>>(op, buf, buf + n, n);
     PK(cudaGetLastError());
     PK(cudaMemcpy(out, buf + n, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost));
     cudaFree(buf);

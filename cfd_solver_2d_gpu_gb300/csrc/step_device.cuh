@@ -60,10 +60,10 @@ __device__ __forceinline__ void alpha_edge(int e, const d4* __restrict__ prim, c
     const double nx = __ldg(&gm[0]), ny = __ldg(&gm[1]), len = __ldg(&gm[2]), sqrt_len = __ldg(&gm[3]);
     const double un = fma(w.y, mul(nx, len), mul(w.z, mul(ny, len)));
     const double ir = rcp(w.x);
-    alpha[e] = fma(sqrt(mul(mul(g.gamma, w.w), ir)), sqrt_len, fabs(un));
+    alpha[e] = fma(sq(mul(mul(g.gamma, w.w), ir)), sqrt_len, fabs(un));
     if (NS) {
         const double T = w.w / g.R * ir;
-        const double mu = g.C1 * (T * sqrt(T)) * rcp(T + 110.4);
+        const double mu = mul(mul(g.C1, mul(T, sq(T))), rcp(T + 110.4));
         alpha_vis[e] = 2.0 * len * value_1 * mu * ir;
     }
 }

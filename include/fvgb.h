@@ -361,11 +361,12 @@ int fvgb_rhs_noalloc(const fvgb_mesh_soa* dev_mesh, const fvgb_params* p, const 
  * kernels bound by the FP64 pipe. */
 int fvgb_fp64_peak(int device, double* gflops);
 
-/* No counterpart in the reference.  The device reciprocal the kernels use in
- * place of most divisions (the hardware approximation refined by a series
- * step) evaluated on n host values x on the given device: out[i] = 1/x[i].
+/* No counterpart in the reference.  The device functions the kernels use in
+ * place of most divisions and square roots (the hardware approximations
+ * refined by a series step) evaluated on n host values x on the given device:
+ * op 0 out[i] = 1/x[i], op 1 out[i] = 1/sqrt(x[i]), op 2 out[i] = sqrt(x[i]).
  * For accuracy tests. */
-int fvgb_math_eval(int device, int n, const double* x, double* out);
+int fvgb_math_eval(int device, int op, int n, const double* x, double* out);
 
 /* No counterpart in the reference.  The correctly rounded FP64 multiply (op 0)
  * and add (op 1) that run on the integer pipes (softfp64.cuh) evaluated on n
