@@ -511,7 +511,26 @@ struct Adjoint {
     long long restricted_before = 0;
     double ms_fwd = 0, ms_bwd = 0;
 
+    // CUDA graphs of a segment's reverse-sweep work (its recorded recomputation, where needed,
+    // and the VJPs of its steps), captured once per shape and replayed: a segment enqueues
+    // several hundred short kernels and copies whose launch gaps the graph removes.  The VJPs
+    // exchange the adjoint buffers d_lam and d_lam_in on the host as they are enqueued, so a
+    // graph belongs to the assignment of the two buffers at the segment's start and records
+    // the assignment it leaves.
+    struct SegGraph {
+        int n = 0;
+        bool rec = false;
+        d4* lam0 = nullptr;
+        d4* lam_out = nullptr;
+        d4* lam_in_out = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        long long launches = 0;
+    };
+    std::vector<SegGraph> seg_graphs;
+
     ~Adjoint() {
+        for (auto& g : seg_graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
         for (void* q : owned) cudaFree(q);
     }
     template <class T>
@@ -865,6 +884,52 @@ struct Adjoint {
         return 0;
     }
 
+    // segment work of the reverse sweep for a segment of n steps (see SegGraph): recomputes
+    // the segment's steps kernel by kernel when rec (its checkpoint already loaded), then runs
+    // the VJPs of its steps from the last to the first
+    int run_segment(int n, bool rec) {
+        Solver& v = *s;
+        for (const SegGraph& g : seg_graphs)
+            if (g.n == n && g.rec == rec && g.lam0 == d_lam) {
+                AK(cudaGraphLaunch(g.exec, v.stream));
+                d_lam = g.lam_out;
+                d_lam_in = g.lam_in_out;
+                v.launches += g.launches;
+                return 0;
+            }
+        SegGraph g;
+        g.n = n;
+        g.rec = rec;
+        g.lam0 = d_lam;
+        d4* const lam_in0 = d_lam_in;
+        const long long before = v.launches;
+        AK(cudaStreamBeginCapture(v.stream, cudaStreamCaptureModeThreadLocal));
+        int rc = 0;
+        if (rec)
+            for (int k = 0; k < n && !rc; k++) rc = record_step(k);
+        for (int k = n - 1; k >= 0 && !rc; k--) rc = step_vjp(k);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(v.stream, &graph);
+        if (rc || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            d_lam = g.lam0;
+            d_lam_in = lam_in0;
+            v.launches = before;
+            return rc ? rc : fail(FVGB_ERR_CUDA, std::string("adjoint graph capture: ") + cudaGetErrorString(e));
+        }
+        g.launches = v.launches - before;
+        v.launches = before;
+        g.lam_out = d_lam;
+        g.lam_in_out = d_lam_in;
+        const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("adjoint graph instantiate: ") + cudaGetErrorString(ei));
+        seg_graphs.push_back(g);
+        AK(cudaGraphLaunch(g.exec, v.stream));
+        v.launches += g.launches;
+        return 0;
+    }
+
     int forward(const double* U0, double t0, double* UK) {
         Solver& v = *s;
         int rc;
@@ -922,10 +987,12 @@ struct Adjoint {
         AK(cudaEventRecord(a, st));
         for (int i = nseg - 1; i >= 0; i--) {
             // the last segment's states are still those the forward sweep recorded
-            if ((i + 1 < nseg || !last_kept) && ((rc = load_segment(i)) || (rc = record_segment(i)))) return rc;
-            const int n = std::min(S, K - i * S);
-            for (int k = n - 1; k >= 0; k--)
-                if ((rc = step_vjp(k))) return rc;
+            const bool rec = i + 1 < nseg || !last_kept;
+            if (rec) {
+                if ((rc = load_segment(i))) return rc;
+                AK(cudaMemcpyAsync(&v.d_state->T, &v.p.T_end, sizeof(double), cudaMemcpyHostToDevice, st));
+            }
+            if ((rc = run_segment(std::min(S, K - i * S), rec))) return rc;
         }
         last_kept = nseg == 1;
         AK(cudaEventRecord(b, st));
