@@ -14,6 +14,7 @@ cell-stage updates per second = cells x 3 x steps / time.  Every array of the
 step is larger than the 129 MB L2, so no flush is needed between steps.
 
 At one GPU the same JSON line also carries the other configurations' records:
+  edge_colour  the same workload with the edge-coloured scatter in place of the gather;
   cylinder_ns  the laminar cylinder O-grid (512 x 256 quads, Navier-Stokes, Kutta RK3);
   batch        256 cylinder O-grids in one persistent launch per stage against the same
                instances stepped one after another through the plain path;
@@ -299,6 +300,39 @@ def run_cylinder(args, quiet=False):
             "config": config(args, N, E, V, "cylinder_ns"), "clocks": clk.summary(), "gpu_launches": launches,
             "roofline": roof, "roofline_stage": stage_roof, "kernel_ms": prof,
             "residual_linf": [float(x) for x in res]}
+    if not quiet:
+        print(json.dumps(line), flush=True)
+    return line
+
+
+def run_colour(args, quiet=False):
+    """The headline workload with the edge-coloured scatter ([gpu] edge_colour = 1: each
+    colour's edges add their fluxes into the cells' sums) in place of the slot-order gather:
+    the side-by-side measurement of the two residual forms on the same mesh."""
+    import torch
+    torch.cuda.set_device(0)
+    import cfd_solver_2d_gpu_gb300 as fv
+    with tempfile.TemporaryDirectory() as d:
+        tp, su2, flux = workload(args, d)
+        p = fv.Params.from_toml(tp)
+        p.edge_colour = 1
+        mesh = fv.Mesh.read_su2(su2, p)
+    N, E, V = mesh.N, mesh.E, mesh.V
+    s = fv.GPUSolver2(mesh, p)
+    _, ncol = s.edge_colours()
+    s.set_time(0.0)
+    s.step_timed(p.T_end, args.warmup)
+    l0 = s.kernel_launches()
+    with ClockSampler(0) as clk:
+        ms = s.step_timed(p.T_end, args.steps)
+    launches = s.kernel_launches() - l0
+    prof = s.profile_steps(p.T_end, max(3, min(args.steps, 20)))
+    s.close()
+    line = {"metric": JSON_METRIC + " [edge-coloured scatter]", "value": 3.0 * N * args.steps / (ms / 1e3),
+            "unit": "cell-stage updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": "f64",
+            "config": dict(config(args, N, E, V), residual="edge-coloured scatter", colours=ncol),
+            "clocks": clk.summary(), "gpu_launches": launches, "kernel_ms": prof}
     if not quiet:
         print(json.dumps(line), flush=True)
     return line
@@ -830,13 +864,16 @@ def main():
                 "e2e": e2e, "cpu_baseline": cpu}
         if world == 1 and not args.no_extras:
             # the other configurations, each measured on its own after the headline run
-            for key, fn in (("cylinder_ns", run_cylinder), ("batch", run_batch), ("adjoint", run_adjoint)):
+            for key, fn in (("edge_colour", run_colour), ("cylinder_ns", run_cylinder), ("batch", run_batch),
+                            ("adjoint", run_adjoint)):
                 t0 = time.perf_counter()
                 try:
                     rec = fn(args, quiet=True)
                 except Exception as exc:  # one record's failure must not hide the headline number
                     rec = {"error": f"{type(exc).__name__}: {exc}"}
                 rec["wall_s"] = time.perf_counter() - t0
+                if key == "edge_colour" and rec.get("value"):
+                    rec["ratio_to_gather"] = rec["value"] / value
                 line[key] = rec
         print(json.dumps(line), flush=True)
 

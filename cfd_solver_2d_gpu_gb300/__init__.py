@@ -38,7 +38,7 @@ class Params(ctypes.Structure):
         (n, ctypes.c_double) for n in ("gamma", "R", "Pr", "mu0", "T0", "CFL", "T_end", "Re")] + [
         ("inf", ctypes.c_double * 4), ("inlet", ctypes.c_double * 4), ("outlet", ctypes.c_double * 4),
         ("vortex", ctypes.c_double * 3), ("shock", ctypes.c_double * 4), ("mesh_scale", ctypes.c_double),
-        ("max_iteration", ctypes.c_int), ("pad_", ctypes.c_int), ("ref_area", ctypes.c_double),
+        ("max_iteration", ctypes.c_int), ("edge_colour", ctypes.c_int), ("ref_area", ctypes.c_double),
         ("dsr", ctypes.c_double * 3), ("dsr_time", ctypes.c_double), ("steady", ctypes.c_int),
         ("pad2_", ctypes.c_int), ("CFL_steady", ctypes.c_double)]
 
@@ -115,6 +115,7 @@ def lib():
             "fvgb_cell_permutation": (i, [v, ip]),
             "fvgb_edge_permutation": (i, [v, ip]),
             "fvgb_layout_connectivity": (i, [v, ip, ip, ip, ip]),
+            "fvgb_edge_colours": (i, [v, ip, ip]),
             "fvgb_kernel_launches": (ctypes.c_longlong, [v]),
             "fvgb_profile_steps": (i, [v, d, i, dp, ip]),
             "fvgb_step_timed": (i, [v, d, i, dp]),
@@ -429,6 +430,13 @@ class GPUSolver2:
         out = np.empty(self.E, dtype=np.int32)
         _check(lib().fvgb_edge_permutation(self._h, _ip(out)))
         return out
+
+    def edge_colours(self):
+        """(colour of each reference edge, number of colours) of [gpu] edge_colour = 1."""
+        out = np.empty(self.E, dtype=np.int32)
+        n = ctypes.c_int()
+        _check(lib().fvgb_edge_colours(self._h, _ip(out), ctypes.byref(n)))
+        return out, n.value
 
     def layout_connectivity(self):
         ee = np.empty((3, self.N), dtype=np.int32)

@@ -548,6 +548,8 @@ struct Adjoint {
         if (p.equation != 1 && p.equation != 2) return fail(FVGB_ERR_ARG, "invalid equation");
         if (p.steady && !rhs_only)
             return fail(FVGB_ERR_UNSUPPORTED, "the adjoint covers time-accurate runs (time.is_steady = 0)");
+        if (p.edge_colour)
+            return fail(FVGB_ERR_UNSUPPORTED, "the adjoint differentiates the gathered residual ([gpu] edge_colour = 0)");
         if (p.flux_scheme != 2001 && p.flux_scheme != 2002) return fail(FVGB_ERR_ARG, "invalid flux scheme");
         if (p.time_advance != 3101 && p.time_advance != 3103 && p.time_advance != 3104)
             return fail(FVGB_ERR_ARG, "invalid time_advance");

@@ -298,9 +298,12 @@ struct Batch {
             for (int i = 0; i < n; i++)
                 if (params[i].mu0 != p.mu0 || params[i].T0 != p.T0 || params[i].Pr != p.Pr)
                     return fail(FVGB_ERR_ARG, "batched Navier-Stokes instances must share mu0, T0 and Pr");
-        for (int i = 0; i < n; i++)
+        for (int i = 0; i < n; i++) {
             if (params[i].steady)
                 return fail(FVGB_ERR_UNSUPPORTED, "the batched form steps in time (time.is_steady = 0)");
+            if (params[i].edge_colour)
+                return fail(FVGB_ERR_UNSUPPORTED, "the batched form gathers the residual ([gpu] edge_colour = 0)");
+        }
         if (p.time_advance != 3101 && p.time_advance != 3103 && p.time_advance != 3104)
             return fail(FVGB_ERR_ARG, "invalid time_advance");
         BK(cudaSetDevice(p.device));

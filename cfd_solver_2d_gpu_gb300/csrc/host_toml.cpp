@@ -357,6 +357,8 @@ extern "C" int fvgb_params_read_toml(const char* path, fvgb_params* p, char* mes
     if (r.str("gpu.restrict", s)) p->restrict_ref = (s == "ref");
     int ren = p->renumber;
     if (r.integer("gpu.renumber", ren, false)) p->renumber = ren;
+    int colour = p->edge_colour;
+    if (r.integer("gpu.edge_colour", colour, false)) p->edge_colour = colour;
     int dev = 0;
     if (r.integer("gpu.device", dev, false)) p->device = dev;
     if (mesh_name && mesh_name_len > 0) {

@@ -274,6 +274,43 @@ int build_layout(const fvgb_mesh_soa& m, const fvgb_params& p, Layout& L) {
         L.dt_edge[fill[L.cell_new[m.edge_L[e]]]++] = L.edge_new[e];
         if (m.edge_R[e] != -1) L.dt_edge[fill[L.cell_new[m.edge_R[e]]]++] = L.edge_new[e];
     }
+    if (p.edge_colour) return build_edge_colours(L);
+    return 0;
+}
+
+// Greedy edge colouring for the coloured scatter: edges visited in device order take the
+// smallest colour that no edge already coloured uses at a cell this edge writes (its L cell,
+// and its R cell where the edge is in R's edge list).  The colours' edge lists keep the device
+// order.  A cell writes at most three edge slots, so at most five colours are needed.
+int build_edge_colours(Layout& L) {
+    const int N = L.N, E = L.E;
+    L.e_in_r.assign(E, 0);
+    for (int c = 0; c < N; c++)
+        for (int j = 0; j < 3; j++) {
+            const int r = L.c_edge[(size_t)c * 3 + j];
+            if (r < 0) L.e_in_r[~r] = 1;
+        }
+    std::vector<uint32_t> used(N, 0u);
+    std::vector<int> colour(E);
+    int nc = 0;
+    for (int e = 0; e < E; e++) {
+        const int l = L.e_L[e], r = L.e_in_r[e] ? L.e_R[e] : -1;
+        const uint32_t busy = used[l] | (r >= 0 ? used[r] : 0u);
+        if (busy == 0xffffffffu) return fail(FVGB_ERR_MESH, "edge colouring needs more than 32 colours");
+        int k = 0;
+        while (busy & (1u << k)) k++;
+        colour[e] = k;
+        used[l] |= 1u << k;
+        if (r >= 0) used[r] |= 1u << k;
+        nc = std::max(nc, k + 1);
+    }
+    L.col_ptr.assign((size_t)nc + 1, 0);
+    for (int e = 0; e < E; e++) L.col_ptr[colour[e] + 1]++;
+    for (int k = 0; k < nc; k++) L.col_ptr[k + 1] += L.col_ptr[k];
+    L.col_edge.resize(E);
+    std::vector<int> fill(L.col_ptr.begin(), L.col_ptr.end() - 1);
+    for (int e = 0; e < E; e++) L.col_edge[fill[colour[e]]++] = e;
+    L.e_colour = colour;
     return 0;
 }
 

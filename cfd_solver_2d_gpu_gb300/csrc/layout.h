@@ -26,11 +26,15 @@ struct Layout {
     std::vector<int> c_ggout;        // [N][3] Green-Gauss outer cell, -1 on boundaries
     std::vector<double> c_ginv;      // [N] 1/vol as the Green-Gauss gradient forms it
     std::vector<int> dt_ptr, dt_edge;  // CSR: edges whose spectral radius a cell sums
+    // edge colouring ([gpu] edge_colour = 1): per edge whether R's edge list holds it, its
+    // colour, and per colour the edges (device order) in col_edge[col_ptr[k] .. col_ptr[k+1])
+    std::vector<int> e_in_r, e_colour, col_ptr, col_edge;
 };
 
 // Checks the caller's mesh arrays (sizes, NULL arrays, every index in range) on the
 // host; FVGB_ERR_MESH with the reason, 0 if the mesh may be indexed.
 int validate_mesh(const fvgb_mesh_soa& m);
 int build_layout(const fvgb_mesh_soa& m, const fvgb_params& p, Layout& L);
+int build_edge_colours(Layout& L);
 
 }  // namespace fvgb

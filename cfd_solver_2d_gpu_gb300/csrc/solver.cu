@@ -140,9 +140,14 @@ int Solver::init(const fvgb_mesh_soa& m, const fvgb_params& prm) {
             (rc = dupload(d_c_ginv, L.c_ginv, owned, s)))
             return rc;
     }
+    if (p.edge_colour &&
+        ((rc = dupload(d_col_edge, L.col_edge, owned, s)) || (rc = dupload(d_e_in_r, L.e_in_r, owned, s))))
+        return rc;
     const size_t n4 = (size_t)N;
+    // the edge fluxes, or in the coloured scatter the cells' sums of them
+    const size_t nF = std::max((size_t)E, p.edge_colour ? n4 : (size_t)0);
     if ((rc = dalloc(d_U, n4, owned)) || (rc = dalloc(d_U0, n4, owned)) || (rc = dalloc(d_Gx, n4, owned)) ||
-        (rc = dalloc(d_Gy, n4, owned)) || (rc = dalloc(d_F, (size_t)E, owned)) || (rc = dalloc(d_prim, n4, owned)) ||
+        (rc = dalloc(d_Gy, n4, owned)) || (rc = dalloc(d_F, nF, owned)) || (rc = dalloc(d_prim, n4, owned)) ||
         (rc = dalloc(d_rhs, n4, owned)) || (rc = dalloc(d_alpha, (size_t)E, owned)) ||
         (rc = dalloc(d_alpha_vis, (size_t)E, owned)) || (rc = dalloc(d_flags, (size_t)kFlagCap, owned)) ||
         (rc = dalloc(d_flag_count, 1, owned)) || (rc = dalloc(d_state, 1, owned)) ||
@@ -234,13 +239,32 @@ void Solver::enqueue_stage(int kind) {
     b.clock_t0 = &d_state->t_old;
     b.clock_dt = &d_state->dt;
     b.clock_frac = dev::dsr_stage_frac(kind);
-    dev::launch_flux(s, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv, gas, b, d_F,
-                     d_status, rec_tape.v ? &rec_tape : nullptr);
+    enqueue_residual(b, kind);
+}
+
+// the edge fluxes and the stage update of one stage: either every edge's flux to d_F and the
+// per-cell gather in the reference's slot order, or ([gpu] edge_colour = 1) the fluxes added
+// colour by colour into the cells' sums in d_F, which the update then reads
+void Solver::enqueue_residual(const dev::BcData& b, int kind) {
+    cudaStream_t s = stream;
+    const bool coloured = p.edge_colour && !rec_tape.v;
+    if (coloured) {
+        cudaMemsetAsync(d_F, 0, sizeof(d4) * (size_t)N, s);
+        const int nc = (int)L.col_ptr.size() - 1;
+        for (int k = 0; k < nc; k++)
+            dev::launch_flux_scatter(s, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv,
+                                     gas, b, d_col_edge + L.col_ptr[k], d_e_in_r, L.col_ptr[k + 1] - L.col_ptr[k],
+                                     d_F, d_status);
+        launches += nc;
+    } else {
+        dev::launch_flux(s, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv, gas, b, d_F,
+                         d_status, rec_tape.v ? &rec_tape : nullptr);
+        launches += (mv.E_int > 0) + (mv.E > mv.E_int);
+    }
     mark(PROF_FLUX, false);
-    launches += (mv.E_int > 0) + (mv.E > mv.E_int);
     mark(PROF_UPDATE, true);
     dev::launch_update(s, kind, d_U, d_U0, d_K1, d_rhs, d_F, mv, d_state, gas, d_flags, d_flag_count, kFlagCap,
-                       d_status, d_rec_R, d_dt_local);
+                       d_status, d_rec_R, d_dt_local, coloured);
     mark(PROF_UPDATE, false);
     launches += 1;
 }
@@ -442,11 +466,7 @@ int Solver::rhs(const double* U, double* R, double* gx, double* gy) {
     b.clock_t0 = &d_state->t;
     b.clock_dt = &d_state->dt;
     b.clock_frac = 0.0;
-    dev::launch_flux(stream, p.flux_scheme, p.reconstruct == 3002, p.equation == 2, d_U, d_Gx, d_Gy, mv, gas, b,
-                     d_F, d_status);
-    dev::launch_update(stream, dev::STAGE_RHS, d_U, d_U0, d_K1, d_rhs, d_F, mv, d_state, gas, d_flags, d_flag_count,
-                       kFlagCap, d_status);
-    launches += 1 + (mv.E_int > 0) + (mv.E > mv.E_int);
+    enqueue_residual(b, dev::STAGE_RHS);
     CK(cudaGetLastError());
     auto out = [&](const d4* src, double* dst) -> int {
         dev::launch_gather_out(stream, src, d_stage, d_cell_new, N);
@@ -619,6 +639,28 @@ extern "C" int fvgb_cell_permutation(fvgb_handle* h, int* perm) {
 extern "C" int fvgb_edge_permutation(fvgb_handle* h, int* perm) {
     if (!h || !perm) return fail(FVGB_ERR_ARG, "null argument");
     std::copy(h->s.L.edge_new.begin(), h->s.L.edge_new.end(), perm);
+    return 0;
+}
+
+extern "C" int fvgb_edge_colours(fvgb_handle* h, int* colour, int* ncolours) {
+    GUARD(h);
+    if (!colour || !ncolours) return fail(FVGB_ERR_ARG, "null argument");
+    Solver& s = h->s;
+    const int E = s.E;
+    std::fill(colour, colour + E, -1);
+    *ncolours = 0;
+    if (!s.p.edge_colour) return 0;
+    // the colour lists as the device holds them, mapped back to the reference's edge numbering
+    std::vector<int> ce(E);
+    CK(cudaMemcpy(ce.data(), s.d_col_edge, sizeof(int) * (size_t)E, cudaMemcpyDeviceToHost));
+    const int nc = (int)s.L.col_ptr.size() - 1;
+    for (int k = 0; k < nc; k++)
+        for (int i = s.L.col_ptr[k]; i < s.L.col_ptr[k + 1]; i++) {
+            const int e = ce[i];
+            if (e < 0 || e >= E) return fail(FVGB_ERR_CUDA, "device colour list holds an edge outside the mesh");
+            colour[s.L.edge_ref[e]] = k;
+        }
+    *ncolours = nc;
     return 0;
 }
 

@@ -40,6 +40,7 @@ struct Solver {
     int* d_c_ggout = nullptr;
     int *d_dt_ptr = nullptr, *d_dt_edge = nullptr;
     int *d_cell_ref = nullptr, *d_cell_new = nullptr;
+    int *d_col_edge = nullptr, *d_e_in_r = nullptr;  // the edge colouring ([gpu] edge_colour = 1)
     // fields
     d4 *d_U = nullptr, *d_U0 = nullptr, *d_K1 = nullptr, *d_Gx = nullptr, *d_Gy = nullptr;
     d4 *d_F = nullptr, *d_prim = nullptr, *d_rhs = nullptr, *d_res_part = nullptr;
@@ -86,6 +87,7 @@ struct Solver {
     int profile_steps(double T, int nsteps, double* ms, int* count);
     bool needs_gradient() const;
     void enqueue_stage(int kind);
+    void enqueue_residual(const dev::BcData& b, int kind);
     void enqueue_step();
     int build_graph();
     void drop_graphs();

@@ -341,12 +341,54 @@ __device__ __forceinline__ d4 flux_rec(const Prim& wL, const Prim& wR, const d4 
     }
 }
 
-// an interior or periodic edge (R reconstructed at the partner's midpoint for periodic ones);
-// with REC (Roe, Euler) the edge's tape entry is written as well
+// the flux of an interior or periodic edge (R reconstructed at the partner's midpoint for
+// periodic ones)
+template <int FLUX, bool LINEAR, bool NS>
+__device__ __forceinline__ d4 flux_interior_value(int e, const d4* __restrict__ U, const d4* __restrict__ Gx,
+                                                  const d4* __restrict__ Gy, const MeshView& m, const Gas& g) {
+    const int L = __ldg(&m.e_L[e]), R = __ldg(&m.e_R[e]);
+    const double2* gm = reinterpret_cast<const double2*>(&m.e_geom[(size_t)e * 8]);
+    const double2 n01 = __ldg(&gm[0]), l23 = __ldg(&gm[1]);
+    const double nx = n01.x, ny = n01.y, len = l23.x;
+    const d4 uL = ld4(&U[L]), uR = ld4(&U[R]);
+    d4 gxL, gyL, gxR, gyR;
+    if (LINEAR || NS) {
+        gxL = ld4(&Gx[L]);
+        gyL = ld4(&Gy[L]);
+        gxR = ld4(&Gx[R]);
+        gyR = ld4(&Gy[R]);
+    }
+    Prim wL, wR;
+    d4 fL, fR;
+    if (LINEAR) {
+        const double2 dL = __ldg(&gm[2]), dR = __ldg(&gm[3]);
+        fL = face_state<true>(uL, gxL, gyL, dL.x, dL.y, g, wL);
+        fR = face_state<true>(uR, gxR, gyR, dR.x, dR.y, g, wR);
+    } else {
+        fL = face_state<false>(uL, gxL, gyL, 0, 0, g, wL);
+        fR = face_state<false>(uR, gxR, gyR, 0, 0, g, wR);
+    }
+    d4 flux = (FLUX == FLUX_ROE) ? roe_flux(wL, wR, fL, fR, nx, ny, len, g) : llf_flux(fL, fR, wL, wR, nx, ny, len, g);
+    if (NS) {
+        // get_U_Gradient_mean / get_U_mean (ViscousFluxGPU.cu:7-87): averages of both sides
+        const d4 ua = mk4(0.5 * (uL.x + uR.x), 0.5 * (uL.y + uR.y), 0.5 * (uL.z + uR.z), 0.5 * (uL.w + uR.w));
+        const d4 gxa = mk4(0.5 * (gxL.x + gxR.x), 0.5 * (gxL.y + gxR.y), 0.5 * (gxL.z + gxR.z), 0.5 * (gxL.w + gxR.w));
+        const d4 gya = mk4(0.5 * (gyL.x + gyR.x), 0.5 * (gyL.y + gyR.y), 0.5 * (gyL.z + gyR.z), 0.5 * (gyL.w + gyR.w));
+        viscous_flux(flux, ua, gxa, gya, nx, ny, len, g);
+    }
+    return flux;
+}
+
+// an interior or periodic edge: its flux to F[e]; with REC (Roe, Euler) the edge's tape entry
+// is written as well
 template <int FLUX, bool LINEAR, bool NS, bool REC = false>
 __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, const d4* __restrict__ Gx,
                                               const d4* __restrict__ Gy, const MeshView& m, const Gas& g,
                                               d4* __restrict__ F, EdgeTape tape = EdgeTape()) {
+    if constexpr (!REC) {
+        F[e] = flux_interior_value<FLUX, LINEAR, NS>(e, U, Gx, Gy, m, g);
+        return;
+    }
     const int L = __ldg(&m.e_L[e]), R = __ldg(&m.e_R[e]);
     const double2* gm = reinterpret_cast<const double2*>(&m.e_geom[(size_t)e * 8]);
     const double2 n01 = __ldg(&gm[0]), l23 = __ldg(&gm[1]);
@@ -380,23 +422,6 @@ __device__ __forceinline__ void flux_interior(int e, const d4* __restrict__ U, c
         F[e] = flux;
         return;
     }
-    if (LINEAR) {
-        const double2 dL = __ldg(&gm[2]), dR = __ldg(&gm[3]);
-        fL = face_state<true>(uL, gxL, gyL, dL.x, dL.y, g, wL);
-        fR = face_state<true>(uR, gxR, gyR, dR.x, dR.y, g, wR);
-    } else {
-        fL = face_state<false>(uL, gxL, gyL, 0, 0, g, wL);
-        fR = face_state<false>(uR, gxR, gyR, 0, 0, g, wR);
-    }
-    d4 flux = (FLUX == FLUX_ROE) ? roe_flux(wL, wR, fL, fR, nx, ny, len, g) : llf_flux(fL, fR, wL, wR, nx, ny, len, g);
-    if (NS) {
-        // get_U_Gradient_mean / get_U_mean (ViscousFluxGPU.cu:7-87): averages of both sides
-        const d4 ua = mk4(0.5 * (uL.x + uR.x), 0.5 * (uL.y + uR.y), 0.5 * (uL.z + uR.z), 0.5 * (uL.w + uR.w));
-        const d4 gxa = mk4(0.5 * (gxL.x + gxR.x), 0.5 * (gxL.y + gxR.y), 0.5 * (gxL.z + gxR.z), 0.5 * (gxL.w + gxR.w));
-        const d4 gya = mk4(0.5 * (gyL.x + gyR.x), 0.5 * (gyL.y + gyR.y), 0.5 * (gyL.z + gyR.z), 0.5 * (gyL.w + gyR.w));
-        viscous_flux(flux, ua, gxa, gya, nx, ny, len, g);
-    }
-    F[e] = flux;
 }
 
 // The double-Mach-reflection boundary (Flux.cpp:21-26 and 280-287): the edge is upstream of
@@ -416,11 +441,67 @@ __device__ __forceinline__ bool dsr_upstream(double x, double y, const BcData& b
 // double Mach reflection); with REC
 // (Roe, Euler) the tape entry of slip-wall, symmetry, far-field, inlet and outlet edges is
 // written as well
+// the flux of a boundary edge with a ghost state (walls, far field, inlet, outlet, symmetry,
+// double Mach reflection)
+template <int FLUX, bool LINEAR, bool NS>
+__device__ __forceinline__ d4 flux_boundary_value(int e, const d4* __restrict__ U, const d4* __restrict__ Gx,
+                                                  const d4* __restrict__ Gy, const MeshView& m, const Gas& g,
+                                                  const BcData& bc, Status* st) {
+    const int L = __ldg(&m.e_L[e]);
+    const int bt = __ldg(&m.e_bc[e]);
+    const double* gm = &m.e_geom[(size_t)e * 8];
+    const double nx = __ldg(&gm[0]), ny = __ldg(&gm[1]), len = __ldg(&gm[2]);
+    const d4 uL = ld4(&U[L]);
+    d4 gxL = mk4(0, 0, 0, 0), gyL = gxL;
+    if (LINEAR || NS) {
+        gxL = ld4(&Gx[L]);
+        gyL = ld4(&Gy[L]);
+    }
+    Prim wL;
+    const d4 fL = face_state<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL);
+    d4 fR = mk4(0, 0, 0, 0);
+    switch (bt) {
+    case BC_SYMMETRY:  // symmetry
+    case BC_WALL_NONVISCOUS:  // slip wall, get_UR_wallNonViscous
+        fR = ghost_slip(fL, wL, nx, ny);
+        break;
+    case BC_WALL_ADIABAT:  // no-slip adiabatic wall, get_UR_wall_adiabat (Flux.cpp:73-79)
+        fR = bc.wall_ref ? mk4(fL.x, -0.0, -0.0, fL.w) : mk4(fL.x, -fL.y, -fL.z, fL.w);
+        break;
+    case BC_INLET:
+        if (!ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
+        break;
+    case BC_OUTLET:
+        if (!ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
+        break;
+    case BC_INF:
+        if (!ghost_farfield(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
+        break;
+    case BC_DSR: {  // boundary edges keep their midpoint in the slots of the absent R offset
+        const bool up = dsr_upstream(__ldg(&gm[6]), __ldg(&gm[7]), bc);
+        const bool ok = up ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
+                           : ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR);
+        if (!ok) atomicAdd(&st->farfield_oor, 1ull);
+        break;
+    }
+    default:
+        break;
+    }
+    const Prim wR = to_prim(fR, g);
+    d4 flux = (FLUX == FLUX_ROE) ? roe_flux(wL, wR, fL, fR, nx, ny, len, g) : llf_flux(fL, fR, wL, wR, nx, ny, len, g);
+    if (NS) viscous_flux(flux, uL, gxL, gyL, nx, ny, len, g);  // boundary: the L cell's values
+    return flux;
+}
+
 template <int FLUX, bool LINEAR, bool NS, bool REC = false>
 __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, const d4* __restrict__ Gx,
                                               const d4* __restrict__ Gy, const MeshView& m, const Gas& g,
                                               const BcData& bc, d4* __restrict__ F, Status* st,
                                               EdgeTape tape = EdgeTape()) {
+    if constexpr (!REC) {
+        F[e] = flux_boundary_value<FLUX, LINEAR, NS>(e, U, Gx, Gy, m, g, bc, st);
+        return;
+    }
     const int L = __ldg(&m.e_L[e]);
     const int bt = __ldg(&m.e_bc[e]);
     const double* gm = &m.e_geom[(size_t)e * 8];
@@ -461,39 +542,8 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
         return;
         }
     }
-    const d4 fL = face_state<LINEAR>(uL, gxL, gyL, __ldg(&gm[4]), __ldg(&gm[5]), g, wL);
-    d4 fR = mk4(0, 0, 0, 0);
-    switch (bt) {
-    case BC_SYMMETRY:  // symmetry
-    case BC_WALL_NONVISCOUS:  // slip wall, get_UR_wallNonViscous
-        fR = ghost_slip(fL, wL, nx, ny);
-        break;
-    case BC_WALL_ADIABAT:  // no-slip adiabatic wall, get_UR_wall_adiabat (Flux.cpp:73-79)
-        fR = bc.wall_ref ? mk4(fL.x, -0.0, -0.0, fL.w) : mk4(fL.x, -fL.y, -fL.z, fL.w);
-        break;
-    case BC_INLET:
-        if (!ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
-        break;
-    case BC_OUTLET:
-        if (!ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
-        break;
-    case BC_INF:
-        if (!ghost_farfield(wL, bc.inf, bc.a_inf, bc.son_inf, nx, ny, g, fR)) atomicAdd(&st->farfield_oor, 1ull);
-        break;
-    case BC_DSR: {  // boundary edges keep their midpoint in the slots of the absent R offset
-        const bool up = dsr_upstream(__ldg(&gm[6]), __ldg(&gm[7]), bc);
-        const bool ok = up ? ghost_farfield(wL, bc.inlet, bc.a_inlet, bc.son_inlet, nx, ny, g, fR)
-                           : ghost_farfield(wL, bc.outlet, bc.a_outlet, bc.son_outlet, nx, ny, g, fR);
-        if (!ok) atomicAdd(&st->farfield_oor, 1ull);
-        break;
-    }
-    default:
-        break;
-    }
-    const Prim wR = to_prim(fR, g);
-    d4 flux = (FLUX == FLUX_ROE) ? roe_flux(wL, wR, fL, fR, nx, ny, len, g) : llf_flux(fL, fR, wL, wR, nx, ny, len, g);
-    if (NS) viscous_flux(flux, uL, gxL, gyL, nx, ny, len, g);  // boundary: the L cell's values
-    F[e] = flux;
+    // kinds the record does not cover: the flux alone
+    F[e] = flux_boundary_value<FLUX, LINEAR, NS>(e, U, Gx, Gy, m, g, bc, st);
 }
 
 // ---- residual gather + stage update.  add_edge_flux_to_element_flux (Flux.cpp:346-392)
@@ -501,21 +551,28 @@ __device__ __forceinline__ void flux_boundary(int e, const d4* __restrict__ U, c
 // calculateFunctionF scales by -1/vol (Evolve.cpp:106-111); the stage combinations
 // are those of Evolve.cpp:12-23 (Euler), 58-86 (Kutta RK3) and the Shu-Osher SSP-RK3.
 // Returns true when the new state needs the positivity pass.
-template <int KIND>
+// With FROM_RES the cell's sum of signed edge fluxes is already in F[c] (the edge-coloured
+// scatter, k_flux_scatter, accumulated it colour by colour) and is read instead of gathered.
+template <int KIND, bool FROM_RES = false>
 __device__ __forceinline__ void update_cell(int c, d4* __restrict__ U, const d4* __restrict__ U0, d4* __restrict__ K1,
                                             d4* __restrict__ rhs_out, const d4* __restrict__ F, const MeshView& m,
                                             double dt, double dt6, const Gas& g, int* __restrict__ flag_list,
                                             unsigned int* flag_count, int flag_cap, Status* st,
                                             d4* __restrict__ rec_R = nullptr) {
-    const int r0 = __ldg(&m.c_edge[c * 3]);
-    const d4 f0 = ld4(&F[r0 >= 0 ? r0 : ~r0]);
-    d4 acc = (r0 >= 0) ? f0 : mk4(-f0.x, -f0.y, -f0.z, -f0.w);  // 0 + s f0 == s f0
+    d4 acc;
+    if constexpr (FROM_RES) {
+        acc = ld4(&F[c]);
+    } else {
+        const int r0 = __ldg(&m.c_edge[c * 3]);
+        const d4 f0 = ld4(&F[r0 >= 0 ? r0 : ~r0]);
+        acc = (r0 >= 0) ? f0 : mk4(-f0.x, -f0.y, -f0.z, -f0.w);  // 0 + s f0 == s f0
 #pragma unroll
-    for (int j = 1; j < 3; j++) {
-        const int r = __ldg(&m.c_edge[c * 3 + j]);
-        const d4 f = ld4(&F[r >= 0 ? r : ~r]);
-        if (r >= 0) { acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w; }
-        else { acc.x -= f.x; acc.y -= f.y; acc.z -= f.z; acc.w -= f.w; }
+        for (int j = 1; j < 3; j++) {
+            const int r = __ldg(&m.c_edge[c * 3 + j]);
+            const d4 f = ld4(&F[r >= 0 ? r : ~r]);
+            if (r >= 0) { acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w; }
+            else { acc.x -= f.x; acc.y -= f.y; acc.z -= f.z; acc.w -= f.w; }
+        }
     }
     const double mv = __ldg(&m.c_mvol[c]);
     const d4 k = mk4(mul(mv, acc.x), mul(mv, acc.y), mul(mv, acc.z), mul(mv, acc.w));

@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(128) k_flux_boundary(const d4* __restrict__ U,
     if (e < m.E) flux_boundary<FLUX, LINEAR, NS, REC>(e, U, Gx, Gy, m, g, bc, F, st, tape);
 }
 
-template <int KIND>
+template <int KIND, bool FROM_RES = false>
 __global__ void __launch_bounds__(256) k_update(d4* __restrict__ U, const d4* __restrict__ U0, d4* __restrict__ K1,
                                                 d4* __restrict__ rhs_out, const d4* __restrict__ F, MeshView m,
                                                 const StepState* s, Gas g, int* __restrict__ flag_list,
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) k_update(d4* __restrict__ U, const d4* __
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= m.N) return;
     if constexpr (KIND == STAGE_LOCAL) {  // evolve_explicit_localtimestep, Evolve.cpp:115-125
-        update_cell<STAGE_EULER>(c, U, U0, K1, rhs_out, F, m, __ldg(&dt_local[c]), 0.0, g, flag_list, flag_count,
+        update_cell<STAGE_EULER, FROM_RES>(c, U, U0, K1, rhs_out, F, m, __ldg(&dt_local[c]), 0.0, g, flag_list, flag_count,
                                  flag_cap, st, rec_R);
         return;
     }
@@ -101,7 +101,31 @@ __global__ void __launch_bounds__(256) k_update(d4* __restrict__ U, const d4* __
         dt = s->dt;
         dt6 = s->dt6;
     }
-    update_cell<KIND>(c, U, U0, K1, rhs_out, F, m, dt, dt6, g, flag_list, flag_count, flag_cap, st, rec_R);
+    update_cell<KIND, FROM_RES>(c, U, U0, K1, rhs_out, F, m, dt, dt6, g, flag_list, flag_count, flag_cap, st, rec_R);
+}
+
+// Edge-coloured scatter: the edges of one colour (no two of them write the same cell) compute
+// their fluxes and add them straight into the cells' sums, +F to L and, where the edge is in R's
+// edge list (interior edges; a periodic edge's partner cell sums its own partner edge), -F to R.
+// The sums are res[c] for the update's FROM_RES form; each cell's sum is taken in colour order.
+template <int FLUX, bool LINEAR, bool NS>
+__global__ void __launch_bounds__(256) k_flux_scatter(const d4* __restrict__ U, const d4* __restrict__ Gx,
+                                                      const d4* __restrict__ Gy, MeshView m, Gas g, BcData bc,
+                                                      const int* __restrict__ edges, const int* __restrict__ in_r,
+                                                      int n, d4* __restrict__ res, Status* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int e = __ldg(&edges[i]);
+    const d4 f = e < m.E_int ? flux_interior_value<FLUX, LINEAR, NS>(e, U, Gx, Gy, m, g)
+                             : flux_boundary_value<FLUX, LINEAR, NS>(e, U, Gx, Gy, m, g, bc, st);
+    const int L = __ldg(&m.e_L[e]);
+    d4 a = res[L];
+    res[L] = mk4(a.x + f.x, a.y + f.y, a.z + f.z, a.w + f.w);
+    if (__ldg(&in_r[e])) {
+        const int R = __ldg(&m.e_R[e]);
+        a = res[R];
+        res[R] = mk4(a.x - f.x, a.y - f.y, a.z - f.z, a.w - f.w);
+    }
 }
 
 // get_local_dt_host/device (CalculateDt.cpp:66-72, 182-186; CalculateDtGPU.cu:83-110): each
@@ -297,11 +321,19 @@ void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, 
 
 void launch_update(cudaStream_t s, int kind, d4* U, const d4* U0, d4* K1, d4* rhs,
                    const d4* F, const MeshView& m, const StepState* st, const Gas& g, int* flag_list,
-                   unsigned int* flag_count, int flag_cap, Status* status, d4* rec_R, const double* dt_local) {
+                   unsigned int* flag_count, int flag_cap, Status* status, d4* rec_R, const double* dt_local,
+                   bool from_res) {
     if (m.N <= 0) return;
     const int b = blocks(m.N, 256);
-#define FVGB_UPD(K) \
-    k_update<K><<<b, 256, 0, s>>>(U, U0, K1, rhs, F, m, st, g, flag_list, flag_count, flag_cap, status, rec_R, dt_local)
+#define FVGB_UPD(K)                                                                                                  \
+    do {                                                                                                             \
+        if (from_res)                                                                                                \
+            k_update<K, true><<<b, 256, 0, s>>>(U, U0, K1, rhs, F, m, st, g, flag_list, flag_count, flag_cap, status, \
+                                                rec_R, dt_local);                                                    \
+        else                                                                                                         \
+            k_update<K><<<b, 256, 0, s>>>(U, U0, K1, rhs, F, m, st, g, flag_list, flag_count, flag_cap, status,       \
+                                          rec_R, dt_local);                                                          \
+    } while (0)
     switch (kind) {
     case STAGE_LOCAL: FVGB_UPD(STAGE_LOCAL); break;
     case STAGE_RHS: FVGB_UPD(STAGE_RHS); break;
@@ -314,6 +346,23 @@ void launch_update(cudaStream_t s, int kind, d4* U, const d4* U0, d4* K1, d4* rh
     default: FVGB_UPD(STAGE_SSP_3); break;
     }
 #undef FVGB_UPD
+}
+
+void launch_flux_scatter(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, const d4* Gx, const d4* Gy,
+                         const MeshView& m, const Gas& g, const BcData& bc, const int* edges, const int* in_r,
+                         int n, d4* res, Status* st) {
+    if (n <= 0) return;
+    const int b = blocks(n, 256);
+#define FVGB_SC(FL, LIN, NSV) \
+    k_flux_scatter<FL, LIN, NSV><<<b, 256, 0, s>>>(U, Gx, Gy, m, g, bc, edges, in_r, n, res, st)
+    if (scheme == FLUX_ROE) {
+        if (linear) { if (ns) FVGB_SC(FLUX_ROE, true, true); else FVGB_SC(FLUX_ROE, true, false); }
+        else { if (ns) FVGB_SC(FLUX_ROE, false, true); else FVGB_SC(FLUX_ROE, false, false); }
+    } else {
+        if (linear) { if (ns) FVGB_SC(FLUX_LLF, true, true); else FVGB_SC(FLUX_LLF, true, false); }
+        else { if (ns) FVGB_SC(FLUX_LLF, false, true); else FVGB_SC(FLUX_LLF, false, false); }
+    }
+#undef FVGB_SC
 }
 
 void launch_restrict(cudaStream_t s, d4* U, const MeshView& m, const int* cell_ref_of_dev,

@@ -30,7 +30,12 @@ void launch_flux(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, 
 void launch_update(cudaStream_t s, int kind, d4* U, const d4* U0, d4* K1, d4* rhs,
                    const d4* F, const MeshView& m, const StepState* st, const Gas& g, int* flag_list,
                    unsigned int* flag_count, int flag_cap, Status* status, d4* rec_R = nullptr,
-                   const double* dt_local = nullptr);
+                   const double* dt_local = nullptr, bool from_res = false);
+// the fluxes of n edges of one colour (edges[0..n)), added into the cells' sums res (+F to L;
+// -F to R where in_r[e]); with launch_update(from_res) in place of the edge-flux gather
+void launch_flux_scatter(cudaStream_t s, int scheme, bool linear, bool ns, const d4* U, const d4* Gx, const d4* Gy,
+                         const MeshView& m, const Gas& g, const BcData& bc, const int* edges, const int* in_r,
+                         int n, d4* res, Status* st);
 void launch_restrict(cudaStream_t s, d4* U, const MeshView& m, const int* cell_ref_of_dev,
                      const int* dev_of_cell_ref, int* flag_list, unsigned int* flag_count, int flag_cap,
                      int restrict_ref, const Gas& g, Status* st);

@@ -57,7 +57,11 @@ typedef struct fvgb_params {
     double shock[4];     /* shock tube: x, y, normal x, normal y (defaults 0, 0, 1, 0) */
     double mesh_scale;   /* constant.mesh_scale_factor */
     int max_iteration;   /* output.maxIteration */
-    int pad_;
+    /* [gpu] edge_colour = 1: the residual is scattered by edge colour (each colour's edges
+     * add their fluxes into the cells' sums; no two edges of a colour share a cell) instead
+     * of gathered per cell in the reference's slot order; the sums then run in colour order.
+     * Plain path only (the batched form and the adjoint refuse it).  Default 0. */
+    int edge_colour;
     double ref_area;     /* constant.referenceArea x mesh_scale_factor (TomlFileManager.cpp:128-131) */
     /* double Mach reflection (initialCondition.doubleShockReflection, FieldInitializer.cpp:93-108):
      * where the shock meets the wall (x, y) and its angle in degrees, [0, 90] */
@@ -220,6 +224,13 @@ int fvgb_device_state(fvgb_handle* h, double** U_dev, int* n_cells);
 /* Cell permutation: perm[i] = this library's index of reference cell i. */
 int fvgb_cell_permutation(fvgb_handle* h, int* perm);
 int fvgb_edge_permutation(fvgb_handle* h, int* perm);
+/* The edge colouring of [gpu] edge_colour = 1 (no counterpart in the reference,
+ * which gathers the residual per cell): colour[i] = the colour of reference edge
+ * i, read back from the device's colour lists, and *ncolours; with the option
+ * off every colour is -1 and *ncolours = 0.  No two edges of a colour write the
+ * same cell (an edge writes its L cell, and its R cell where it is one of R's
+ * edges: interior edges, not periodic or boundary ones). */
+int fvgb_edge_colours(fvgb_handle* h, int* colour, int* ncolours);
 /* Device-side layout arrays mapped back to reference numbering, for checking
  * connectivity: elem_edges[3][N] (slot order), elem_neighbors[3][N] (the
  * valid face neighbours in slot order, then -1, as the gradient reads them),
