@@ -73,6 +73,15 @@ __device__ __forceinline__ bool is_nan(double x) {
     return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
 
+// -x and |x| as sign-bit operations on the integer pipe (exact; NaN payloads kept), where
+// the compiler would otherwise materialise them with an FP64 add
+__device__ __forceinline__ double negd(double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+__device__ __forceinline__ double absd(double x) {
+    return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+}
+
 // a * b, rounded once to nearest even, never contracted into a fused multiply-add
 __device__ __forceinline__ double mul(double a, double b) {
 #if FVGB_SOFT_MUL
@@ -188,7 +197,7 @@ __device__ __forceinline__ d4 roe_core(const Prim& L, const Prim& R, const d4 UL
     const double iam = rsq(am2);
     const double am = mul(am2, iam);
     const double un = fma(um, nx, mul(vm, ny));
-    const double eig1 = fabs(un);
+    const double eig1 = absd(un);
     const bool sub = dlt(eig1, am);                      // |un| < am
     const double astar = sub ? am : eig1;                // (eig2 + eig3) / 2 = dmax(eig1, am)
     const double sel = sub ? un : copysign(am, un);
@@ -233,8 +242,8 @@ __device__ __forceinline__ d4 llf_flux(const d4 UL, const d4 UR, const Prim& L, 
     const double ruL = fma(nx, UL.y, mul(ny, UL.z)), ruR = fma(nx, UR.y, mul(ny, UR.z));
     const double hl = mul(UL.w + L.p, L.ir);
     const double hr = mul(UR.w + R.p, R.ir);
-    const double aL = fabs(unL) + sq(mul(mul(g.gamma, L.p), L.ir));
-    const double aR = fabs(unR) + sq(mul(mul(g.gamma, R.p), R.ir));
+    const double aL = absd(unL) + sq(mul(mul(g.gamma, L.p), L.ir));
+    const double aR = absd(unR) + sq(mul(mul(g.gamma, R.p), R.ir));
     const double lm = dmax(aL, aR);
     const double hlen = mul(0.5, length);
     return mk4(mul(hlen, ruL + ruR - mul(lm, UR.x - UL.x)),

@@ -60,7 +60,7 @@ __device__ __forceinline__ void alpha_edge(int e, const d4* __restrict__ prim, c
     const double nx = __ldg(&gm[0]), ny = __ldg(&gm[1]), len = __ldg(&gm[2]), sqrt_len = __ldg(&gm[3]);
     const double un = fma(w.y, mul(nx, len), mul(w.z, mul(ny, len)));
     const double ir = rcp(w.x);
-    alpha[e] = fma(sq(mul(mul(g.gamma, w.w), ir)), sqrt_len, fabs(un));
+    alpha[e] = fma(sq(mul(mul(g.gamma, w.w), ir)), sqrt_len, absd(un));
     if (NS) {
         const double T = w.w / g.R * ir;
         const double mu = mul(mul(g.C1, mul(T, sq(T))), rcp(T + 110.4));
@@ -565,13 +565,15 @@ __device__ __forceinline__ void update_cell(int c, d4* __restrict__ U, const d4*
     } else {
         const int r0 = __ldg(&m.c_edge[c * 3]);
         const d4 f0 = ld4(&F[r0 >= 0 ? r0 : ~r0]);
-        acc = (r0 >= 0) ? f0 : mk4(-f0.x, -f0.y, -f0.z, -f0.w);  // 0 + s f0 == s f0
+        acc = (r0 >= 0) ? f0 : mk4(negd(f0.x), negd(f0.y), negd(f0.z), negd(f0.w));  // 0 + s f0 == s f0
 #pragma unroll
         for (int j = 1; j < 3; j++) {
+            // a - f == a + (-f) exactly: the sign is flipped on the integer pipe and each
+            // component costs one FP64 add whichever side the cell is on
             const int r = __ldg(&m.c_edge[c * 3 + j]);
-            const d4 f = ld4(&F[r >= 0 ? r : ~r]);
-            if (r >= 0) { acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w; }
-            else { acc.x -= f.x; acc.y -= f.y; acc.z -= f.z; acc.w -= f.w; }
+            d4 f = ld4(&F[r >= 0 ? r : ~r]);
+            if (r < 0) f = mk4(negd(f.x), negd(f.y), negd(f.z), negd(f.w));
+            acc.x += f.x; acc.y += f.y; acc.z += f.z; acc.w += f.w;
         }
     }
     const double mv = __ldg(&m.c_mvol[c]);

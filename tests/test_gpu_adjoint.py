@@ -85,7 +85,8 @@ def test_adjoint_matches_fd_second_order_ssp(tmp_path):
     K = 10
     rho_t = forward(solver, p, Ut0, K)[0]
     errs, _ = fd_check(solver, p, U0, rho_t, K, 8)
-    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+    print(f"FD relative errors: median {np.median(errs):.2e} max {errs.max():.2e} over {len(errs)} directions")
+    assert np.median(errs) <= 1e-6 and errs.max() <= 2e-5, errs  # measured: median 1.3e-7, max 2.3e-6
 
 
 def test_adjoint_matches_fd_first_order_euler(tmp_path):
@@ -93,6 +94,7 @@ def test_adjoint_matches_fd_first_order_euler(tmp_path):
     K = 8
     rho_t = forward(solver, p, Ut0, K)[0]
     errs, _ = fd_check(solver, p, U0, rho_t, K, 6)
+    print(f"FD relative errors: median {np.median(errs):.2e} max {errs.max():.2e} over {len(errs)} directions")
     assert errs.max() <= 1e-6, errs
 
 
@@ -101,7 +103,8 @@ def test_adjoint_slip_walls(tmp_path):
     K = 6
     rho_t = forward(solver, p, Ut0, K)[0]
     errs, _ = fd_check(solver, p, U0, rho_t, K, 6)
-    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+    print(f"FD relative errors: median {np.median(errs):.2e} max {errs.max():.2e} over {len(errs)} directions")
+    assert np.median(errs) <= 1e-7 and errs.max() <= 1e-6, errs  # measured: median 8.5e-9, max 1.6e-8
 
 
 def test_checkpoints_do_not_change_the_gradient(tmp_path):
@@ -133,7 +136,8 @@ def test_against_oracle_finite_differences(tmp_path):
         Lp, _ = loss_seed(o.run(U0 + H * d, K)[0], rho_t)
         Lm, _ = loss_seed(o.run(U0 - H * d, K)[0], rho_t)
         fd = (Lp - Lm) / (2 * H)
-        assert abs(fd - np.sum(g * d)) <= 1e-5 * abs(fd)
+        print(f"oracle FD relative error {abs(fd - np.sum(g * d)) / abs(fd):.2e}")
+        assert abs(fd - np.sum(g * d)) <= 1e-6 * abs(fd)  # measured: 7e-10 .. 2.2e-8
 
 
 def test_torch_autograd_function(tmp_path):
@@ -174,7 +178,8 @@ def test_adjoint_matches_fd_kutta_rk3(tmp_path):
     K = 8
     rho_t = forward(solver, p, Ut0, K)[0]
     errs, _ = fd_check(solver, p, U0, rho_t, K, 6)
-    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+    print(f"FD relative errors: median {np.median(errs):.2e} max {errs.max():.2e} over {len(errs)} directions")
+    assert np.median(errs) <= 1e-7 and errs.max() <= 1e-6, errs  # measured: median 9.4e-9, max 2.2e-8
 
 
 @pytest.mark.parametrize("flux,gradient", [(2001, 1), (2002, 2), (2001, 2)])
@@ -185,7 +190,8 @@ def test_adjoint_llf_and_green_gauss(tmp_path, flux, gradient):
     K = 8
     rho_t = forward(solver, p, Ut0, K)[0]
     errs, _ = fd_check(solver, p, U0, rho_t, K, 6)
-    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+    print(f"FD relative errors: median {np.median(errs):.2e} max {errs.max():.2e} over {len(errs)} directions")
+    assert np.median(errs) <= 1e-7 and errs.max() <= 2e-6, errs  # measured: medians <= 2.9e-8, max <= 1.0e-7
 
 
 def boundary_case(tmp_path, name, text, su2):
@@ -249,7 +255,11 @@ def test_adjoint_far_field_inlet_outlet(tmp_path, kind):
     rho_t = forward(solver, p, Ut0, K)[0]
     errs, g = fd_check(solver, p, U0, rho_t, K, 6)
     assert np.all(np.isfinite(g))
-    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+    print(f"FD relative errors: median {np.median(errs):.2e} max {errs.max():.2e} over {len(errs)} directions")
+    # measured maxima: cylinder 3.8e-7, channels 5.4e-9 .. 1.4e-7, double Mach reflection 5.9e-6 (its
+    # moving shock switches "dsr" edges between the inlet and outlet states near the FD step)
+    bound = 5e-5 if kind == "channel_dsr" else 5e-6
+    assert np.median(errs) <= 1e-7 and errs.max() <= bound, errs
 
 
 @pytest.mark.parametrize("kind", ["vortex_ns", "channel_ns_gg", "channel_ns_o1_mirror"])
@@ -277,7 +287,13 @@ def test_adjoint_navier_stokes(tmp_path, kind):
     rho_t = forward(solver, p, Ut0, K)[0]
     errs, g = fd_check(solver, p, U0, rho_t, K, 6)
     assert np.all(np.isfinite(g))
-    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+    print(f"FD relative errors: median {np.median(errs):.2e} max {errs.max():.2e} over {len(errs)} directions")
+    # measured: vortex_ns median 9.5e-7, max 1.0e-5 (limiter branches of the viscous vortex near the
+    # FD step); the channels' maxima 6.1e-8 and 1.1e-7
+    if kind == "vortex_ns":
+        assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+    else:
+        assert np.median(errs) <= 1e-7 and errs.max() <= 2e-6, errs
 
 
 @pytest.mark.parametrize("kind", ["vortex_lsq_barth_roe", "vortex_gg_llf", "vortex_o1", "channel_subsonic",
@@ -318,7 +334,8 @@ def test_rhs_vjp_matches_fd(tmp_path, kind):
         ad = float(np.sum(g * dU))
         errs.append(abs(fd - ad) / max(abs(fd), 1e-30))
     errs = np.array(errs)
-    assert np.median(errs) <= 1e-6 and errs.max() <= 1e-4, errs
+    print(f"FD relative errors: median {np.median(errs):.2e} max {errs.max():.2e} over {len(errs)} directions")
+    assert np.median(errs) <= 1e-7 and errs.max() <= 1e-6, errs  # measured: maxima 5.2e-9 .. 4.1e-8
 
 
 def test_handles_in_parallel_threads(tmp_path):
