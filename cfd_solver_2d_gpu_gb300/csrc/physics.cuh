@@ -73,13 +73,26 @@ __device__ __forceinline__ bool is_nan(double x) {
     return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
 
-// -x and |x| as sign-bit operations on the integer pipe (exact; NaN payloads kept), where
-// the compiler would otherwise materialise them with an FP64 add
+// -x, |x| and copysign(x, y) as sign-bit operations on the integer pipe (exact; NaN
+// payloads kept).  Written in C++ -- a unary minus, fabs, or even an integer XOR or AND of
+// the bits -- the compiler issues them as an FP64 add, one FP64-pipe slot each; inline PTX
+// keeps them on the integer pipe.
 __device__ __forceinline__ double negd(double x) {
-    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+    double r;
+    asm("{ .reg .b64 t; mov.b64 t, %1; xor.b64 t, t, 0x8000000000000000; mov.b64 %0, t; }" : "=d"(r) : "d"(x));
+    return r;
 }
 __device__ __forceinline__ double absd(double x) {
-    return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+    double r;
+    asm("{ .reg .b64 t; mov.b64 t, %1; and.b64 t, t, 0x7fffffffffffffff; mov.b64 %0, t; }" : "=d"(r) : "d"(x));
+    return r;
+}
+__device__ __forceinline__ double copysignd(double x, double y) {
+    double r;
+    asm("{ .reg .b64 a, b; mov.b64 a, %1; mov.b64 b, %2; and.b64 a, a, 0x7fffffffffffffff;"
+        " and.b64 b, b, 0x8000000000000000; or.b64 a, a, b; mov.b64 %0, a; }"
+        : "=d"(r) : "d"(x), "d"(y));
+    return r;
 }
 
 // a * b, rounded once to nearest even, never contracted into a fused multiply-add
@@ -200,7 +213,7 @@ __device__ __forceinline__ d4 roe_core(const Prim& L, const Prim& R, const d4 UL
     const double eig1 = absd(un);
     const bool sub = dlt(eig1, am);                      // |un| < am
     const double astar = sub ? am : eig1;                // (eig2 + eig3) / 2 = dmax(eig1, am)
-    const double sel = sub ? un : copysign(am, un);
+    const double sel = sub ? un : copysignd(am, un);
     const double Mstar = mul(sel, iam);                  // (eig2 - eig3) / (2 am)
     const double dE = fma(UR.w, R.ir, -mul(UL.w, L.ir));  // (HR - ER) - (HL - EL)
     const double Etm = fma(g.Etm_c, Vm2, mul(Hm, g.inv_gamma));

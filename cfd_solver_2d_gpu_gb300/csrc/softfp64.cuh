@@ -30,9 +30,14 @@
 namespace fvgb {
 namespace soft {
 
+// The bit moves go through inline PTX on the device: the compiler recognises a bit cast
+// followed by a sign mask or flip as fabs or negation and issues it as an FP64 instruction,
+// on the pipe these functions exist to relieve.
 __host__ __device__ __forceinline__ uint64_t bits_of(double x) {
 #if defined(__CUDA_ARCH__)
-    return (uint64_t)__double_as_longlong(x);
+    uint64_t u;
+    asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+    return u;
 #else
     uint64_t u;
     memcpy(&u, &x, sizeof u);
@@ -41,7 +46,9 @@ __host__ __device__ __forceinline__ uint64_t bits_of(double x) {
 }
 __host__ __device__ __forceinline__ double double_of(uint64_t u) {
 #if defined(__CUDA_ARCH__)
-    return __longlong_as_double((long long)u);
+    double x;
+    asm("mov.b64 %0, %1;" : "=d"(x) : "l"(u));
+    return x;
 #else
     double x;
     memcpy(&x, &u, sizeof x);

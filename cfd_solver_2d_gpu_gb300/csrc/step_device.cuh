@@ -568,8 +568,8 @@ __device__ __forceinline__ void update_cell(int c, d4* __restrict__ U, const d4*
         acc = (r0 >= 0) ? f0 : mk4(negd(f0.x), negd(f0.y), negd(f0.z), negd(f0.w));  // 0 + s f0 == s f0
 #pragma unroll
         for (int j = 1; j < 3; j++) {
-            // a - f == a + (-f) exactly: the sign is flipped on the integer pipe and each
-            // component costs one FP64 add whichever side the cell is on
+            // a - f == a + (-f) exactly: the sign flipped on the integer pipe (negd), one FP64
+            // add a component whichever side of the edge the cell is on
             const int r = __ldg(&m.c_edge[c * 3 + j]);
             d4 f = ld4(&F[r >= 0 ? r : ~r]);
             if (r < 0) f = mk4(negd(f.x), negd(f.y), negd(f.z), negd(f.w));
