@@ -57,7 +57,9 @@ __device__ __forceinline__ void roe_rev(const Prim& L, const Prim& R, const d4 U
     const double h = mul(0.5, area);
     // ---- reverse ----
     const double bC0 = mul(h, bF.x), bC1 = mul(h, bF.y), bC2 = mul(h, bF.z), bC3 = mul(h, bF.w);  // central part
-    const double bD0 = -bC0, bD1 = -bC1, bD2 = -bC2, bD3 = -bC3;                                    // dissipation
+    // dissipation: the sign flips on the integer pipe (negd), since these feed integer-pipe
+    // products that cannot absorb a negation the way an FP64 instruction's operand does
+    const double bD0 = negd(bC0), bD1 = negd(bC1), bD2 = negd(bC2), bD3 = negd(bC3);
     double b_eig1 = fma(bD3, dW3, fma(bD2, dW2, fma(bD1, dW1, mul(bD0, dW0))));
     double b_dW0 = mul(bD0, eig1);
     const double b_dW1 = mul(bD1, eig1), b_dW2 = mul(bD2, eig1), b_dW3 = mul(bD3, eig1);

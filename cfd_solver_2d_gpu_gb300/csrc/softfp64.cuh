@@ -15,9 +15,10 @@
 // operations": the product and the sum, with a sticky bit folded into the
 // least significant bit of the aligned operand).  Only the common case is
 // handled here: finite normal operands whose result is normal (and, for the
-// sum, not an exact zero).  Every other case -- zeros, subnormals, infinities,
-// NaN, results that underflow or overflow -- calls the hardware instruction,
-// so the functions are total.  The probe kernels in probe.cu test them bit for
+// sum, not an exact zero), and for the product also a zero times a finite
+// number.  Every other case -- other zeros, subnormals, infinities, NaN,
+// results that underflow or overflow -- calls the hardware instruction, so the
+// functions are total.  The probe kernels in probe.cu test them bit for
 // bit against the hardware instructions and time them.
 //
 // The functions compile for the host as well (the fallback is then the host's
@@ -93,8 +94,13 @@ __host__ __device__ __forceinline__ double dmul(double a, double b) {
     const int ea = (int)((ha >> 20) & 0x7ffu), eb = (int)((hb >> 20) & 0x7ffu);
     const int e = ea + eb - 1023;  // biased exponent when the significands' product lies in [1, 2)
     // normal operands and a normal result even after a normalising shift and a rounding carry
-    if (!((unsigned)(ea - 1) < 2046u && (unsigned)(eb - 1) < 2046u && (unsigned)(e - 1) < 2044u))
+    if (!((unsigned)(ea - 1) < 2046u && (unsigned)(eb - 1) < 2046u && (unsigned)(e - 1) < 2044u)) {
+        // a zero times a finite number is a zero with the sign of the product: common where
+        // a field is uniform or an adjoint is zero, and no reason to leave the integer pipe
+        const bool za = (ua << 1) == 0ull, zb = (ub << 1) == 0ull;
+        if ((za && eb != 0x7ff) || (zb && ea != 0x7ff)) return double_of((ua ^ ub) & kSign);
         return mul_rare(a, b);
+    }
     // significands ma 2^32 + la and mb 2^32 + lb (53 bits each, hidden bit set)
     const uint32_t la = (uint32_t)ua, lb = (uint32_t)ub;
     const uint32_t ma = (ha & 0xfffffu) | 0x100000u, mb = (hb & 0xfffffu) | 0x100000u;
