@@ -410,7 +410,7 @@ def run_adjoint(args, quiet=False):
     import torch
     torch.cuda.set_device(0)
     import cfd_solver_2d_gpu_gb300 as fv
-    from cfd_solver_2d_gpu_gb300 import adjoint_backward, adjoint_forward, cases
+    from cfd_solver_2d_gpu_gb300 import adjoint_backward, adjoint_forward, adjoint_overlap, cases
     K = args.adjoint_k
     with tempfile.TemporaryDirectory() as d:
         su2 = cases.square_mesh(256, jitter=0.2, directory=d)
@@ -450,6 +450,12 @@ def run_adjoint(args, quiet=False):
             seed[0] = dd
             g, ms_b = adjoint_backward(s, seed)
             wall = time.perf_counter() - t0
+            overlapped = adjoint_overlap(s)
+            # the same sweeps with recomputation and reverse one after the other (one set of records)
+            adjoint_overlap(s, 0)
+            UK_seq, ms_f_seq = adjoint_forward(s, U0, K, nck)
+            g_seq, ms_b_seq = adjoint_backward(s, seed)
+            adjoint_overlap(s, 1)
         L0 = 0.5 * float(dd @ dd)
 
         def loss(U):
@@ -521,6 +527,13 @@ def run_adjoint(args, quiet=False):
             "clocks": clk.summary(),
             "primal_ms": ms_primal, "adjoint_forward_ms": ms_f, "adjoint_backward_ms": ms_b,
             "ratio_backward_to_primal": ms_b / ms_primal, "wall_s": wall, "loss": L0,
+            "overlap": {"used": overlapped,
+                        "note": "each segment's recomputation on the solver's stream beside the reverse of the "
+                                "next segment on a second stream (two sets of records); sequential: one set, "
+                                "recomputation then reverse, same run",
+                        "sequential_forward_ms": ms_f_seq, "sequential_backward_ms": ms_b_seq,
+                        "sequential_value": (ms_f_seq - ms_primal + ms_b_seq) / ms_primal,
+                        "bitwise_equal": bool(np.array_equal(g_seq, g) and np.array_equal(UK_seq, UK))},
             "fd": {"step": h, "directions": len(errs),
                    "median_rel_err": float(np.median(errs)) if len(errs) else None,
                    "max_rel_err": float(errs.max()) if len(errs) else None,

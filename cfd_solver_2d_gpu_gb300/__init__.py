@@ -529,7 +529,21 @@ def _bind_adjoint():
     L.fvgb_adjoint_backward.argtypes = [ctypes.c_void_p, dp, dp, dp]
     L.fvgb_adjoint_release.restype = None
     L.fvgb_adjoint_release.argtypes = [ctypes.c_void_p]
+    L.fvgb_adjoint_overlap.restype = ctypes.c_int
+    L.fvgb_adjoint_overlap.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     return L
+
+
+def adjoint_overlap(solver, mode=None):
+    """Sets (mode 1 or 0, from the next adjoint_forward) whether the backward sweep recomputes
+    each segment beside the reverse of the next on a second stream; returns whether the
+    current adjoint workspace does (False before the first adjoint_forward)."""
+    L = _bind_adjoint()
+    if mode is not None:
+        solver._adj_overlap = 1 if mode else 0
+    cur = ctypes.c_int()
+    _check(L.fvgb_adjoint_overlap(solver._h, getattr(solver, "_adj_overlap", 1), ctypes.byref(cur)))
+    return bool(cur.value)
 
 
 def adjoint_forward(solver, U0, nsteps, n_checkpoints=None, t0=0.0):

@@ -15,7 +15,13 @@
 // reverse sweep each segment is recomputed once, keeping per step U_0, U_1, U_2,
 // the stages' residuals, edge tapes and limiter records, so the sweep costs one
 // extra forward pass and about K/S 4N + S (74 N + 117 E) doubles (sqrt(K)
-// checkpoints: O(sqrt(K) N)).
+// checkpoints: O(sqrt(K) N)).  Where the device has room for a second set of segment
+// records (and fvgb_adjoint_overlap has not turned it off), the recomputation of segment
+// i-1 runs on the solver's stream beside the reverse sweep of segment i on a second,
+// higher-priority stream: both are branches of one CUDA graph, and the two sets of records
+// alternate.  The kernels and their inputs are the same either way, so the gradient is
+// bitwise the same; the small per-stage kernels of a 10^5-cell mesh leave enough of the
+// SMs idle for the two sweeps to share them.
 //
 // Kernels of one stage VJP (all gathers, no atomics: deterministic):
 //   k_adj_edge     per edge: mu = seed-weighted flux adjoint, flux VJP from the stage's tape
@@ -507,7 +513,17 @@ struct Adjoint {
     double* d_dotp = nullptr;
     double* d_one = nullptr;  // 1.0: the time step of rhs_vjp's reverse
     bool ready = false;
-    bool last_kept = false;  // the segment buffers hold the last segment's steps
+    bool last_kept = false;  // the segment buffers (set 0) hold the last segment's steps
+    // segment records: nsets sets of S steps x nst stages; record_step writes set rec_set,
+    // step_vjp reads set rev_set
+    int nsets = 1, rec_set = 0, rev_set = 0;
+    cudaStream_t rstream = nullptr;     // the reverse sweep's stream beside a recomputation
+    cudaStream_t vjp_stream = nullptr;  // where the VJPs are enqueued (null: the solver's stream)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    size_t at(int set, int slot, int si) const { return ((size_t)set * S + slot) * nst + si; }
+    size_t step_at(int set, int slot) const { return (size_t)set * S + slot; }
+    cudaStream_t vstream() const { return vjp_stream ? vjp_stream : s->stream; }
+    int seg_len(int i) const { return std::min(S, K - i * S); }
     long long restricted_before = 0;
     double ms_fwd = 0, ms_bwd = 0;
 
@@ -518,8 +534,10 @@ struct Adjoint {
     // graph belongs to the assignment of the two buffers at the segment's start and records
     // the assignment it leaves.
     struct SegGraph {
-        int n = 0;
-        bool rec = false;
+        int n = 0;        // steps reversed
+        int nrec = 0;     // steps recorded (before the reverse, or beside it when overlap)
+        bool overlap = false;
+        int rev = 0, rec = 0;  // the record sets read and written
         d4* lam0 = nullptr;
         d4* lam_out = nullptr;
         d4* lam_in_out = nullptr;
@@ -532,12 +550,36 @@ struct Adjoint {
         for (auto& g : seg_graphs)
             if (g.exec) cudaGraphExecDestroy(g.exec);
         for (void* q : owned) cudaFree(q);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (rstream) cudaStreamDestroy(rstream);
     }
     template <class T>
     int alloc(T*& p, size_t n) {
         p = nullptr;
         AK(cudaMalloc((void**)&p, (n ? n : 1) * sizeof(T)));
         owned.push_back((void*)p);
+        return 0;
+    }
+
+    // the records of one segment (S steps x nst stages) in set `set`
+    int alloc_set(int set) {
+        const int N = s->N, E = s->E;
+        int rc;
+        for (int k = 0; k < S; k++)
+            for (int si = 0; si < nst; si++) {
+                const size_t i = at(set, k, si);
+                if ((rc = alloc(seg_states[i], N)) || (rc = alloc(seg_R[i], N)) ||
+                    (rc = alloc(seg_tape[i], (size_t)dev::kTapeFields * E)) || (rc = alloc(seg_tflags[i], E)))
+                    return rc;
+                if (!seg_gx.empty() && ((rc = alloc(seg_gx[i], N)) || (rc = alloc(seg_gy[i], N)))) return rc;
+                if (!seg_ctape.empty()) {
+                    dev::CellTape& t = seg_ctape[i];
+                    if ((rc = alloc(t.gx, N)) || (rc = alloc(t.gy, N)) || (rc = alloc(t.phi, N)) ||
+                        (rc = alloc(t.rden, N)) || (rc = alloc(t.code, N)))
+                        return rc;
+                }
+            }
         return 0;
     }
 
@@ -587,31 +629,39 @@ struct Adjoint {
         for (int i = 0; i < nseg; i++)
             if ((rc = alloc(chk[i], N))) return rc;
         if ((rc = alloc(d_chk_t, nseg))) return rc;
-        seg_states.assign((size_t)S * nst, nullptr);
-        for (auto& q : seg_states)
-            if ((rc = alloc(q, N))) return rc;
-        seg_R.assign((size_t)S * nst, nullptr);
-        for (auto& q : seg_R)
-            if ((rc = alloc(q, N))) return rc;
-        seg_tape.assign((size_t)S * nst, nullptr);
-        seg_tflags.assign((size_t)S * nst, nullptr);
-        for (size_t i = 0; i < seg_tape.size(); i++)
-            if ((rc = alloc(seg_tape[i], (size_t)dev::kTapeFields * E)) || (rc = alloc(seg_tflags[i], E))) return rc;
+        // two sets of segment records are laid out; the second is allocated only where it fits
         const bool grads = p.reconstruct == 3002 || p.equation == 2;  // the step computes gradients
-        seg_ctape.assign(grads && p.limiter == 1 ? (size_t)S * nst : 0, dev::CellTape());
+        const size_t per = (size_t)S * nst;
+        seg_states.assign(2 * per, nullptr);
+        seg_R.assign(2 * per, nullptr);
+        seg_tape.assign(2 * per, nullptr);
+        seg_tflags.assign(2 * per, nullptr);
+        seg_ctape.assign(grads && p.limiter == 1 ? 2 * per : 0, dev::CellTape());
         if (p.equation == 2) {
-            seg_gx.assign((size_t)S * nst, nullptr);
-            seg_gy.assign((size_t)S * nst, nullptr);
-            for (size_t i = 0; i < seg_gx.size(); i++)
-                if ((rc = alloc(seg_gx[i], N)) || (rc = alloc(seg_gy[i], N))) return rc;
+            seg_gx.assign(2 * per, nullptr);
+            seg_gy.assign(2 * per, nullptr);
             if ((rc = alloc(d_avu, E)) || (rc = alloc(d_avgx, E)) || (rc = alloc(d_avgy, E))) return rc;
         }
-        for (auto& t : seg_ctape)
-            if ((rc = alloc(t.gx, N)) || (rc = alloc(t.gy, N)) || (rc = alloc(t.phi, N)) || (rc = alloc(t.rden, N)) ||
-                (rc = alloc(t.code, N)))
-                return rc;
+        const bool want2 = !rhs_only && s->adj_overlap && nseg > 1;
+        size_t free0 = 0, free1 = 0, total = 0;
+        if (want2) AK(cudaMemGetInfo(&free0, &total));
+        if ((rc = alloc_set(0))) return rc;
+        nsets = 1;
+        if (want2) {
+            AK(cudaMemGetInfo(&free1, &total));
+            const size_t used = free0 > free1 ? free0 - free1 : 0;
+            if (free1 > used + ((size_t)1 << 30)) {  // room for a second set and 1 GiB besides
+                if ((rc = alloc_set(1))) return rc;
+                int least = 0, greatest = 0;
+                AK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+                AK(cudaStreamCreateWithPriority(&rstream, cudaStreamNonBlocking, greatest));
+                AK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+                AK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+                nsets = 2;
+            }
+        }
         const int nb = nblk(N, 256);
-        if ((rc = alloc(d_seg_dt, 2 * (size_t)S)) || (rc = alloc(d_seg_cstar, S)) || (rc = alloc(d_lam, N)) ||
+        if ((rc = alloc(d_seg_dt, 4 * (size_t)S)) || (rc = alloc(d_seg_cstar, 2 * (size_t)S)) || (rc = alloc(d_lam, N)) ||
             (rc = alloc(d_lam_in, N)) || (rc = alloc(d_acc0, N)) || (rc = alloc(d_aL, E)) || (rc = alloc(d_aR, E)) ||
             (rc = alloc(d_lamdir, N)) || (rc = alloc(d_keepU, N)) || (rc = alloc(d_bdU, 3 * (size_t)N)) ||
             (rc = alloc(d_dotp, (size_t)nb * 3)))
@@ -653,29 +703,29 @@ struct Adjoint {
         Solver& v = *s;
         cudaStream_t st = v.stream;
         const bool copy = v.p.time_advance != 3101;
-        AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
+        AK(cudaMemcpyAsync(seg_states[at(rec_set, slot, 0)], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
         dev::launch_prim(st, v.d_U, v.d_U0, v.d_prim, v.N, v.gas, copy);
         const double value_1 = std::max(4.0 / 3.0, v.p.gamma / v.p.Pr);
         dev::launch_dt(st, v.d_prim, v.mv, v.gas, value_1, v.p.CFL, v.p.equation == 2, v.d_alpha, v.d_alpha_vis,
                        &v.d_state->dtmin_bits, v.d_status);
-        AK(cudaMemsetAsync(d_seg_cstar + slot, 0x7f, sizeof(int), st));
+        AK(cudaMemsetAsync(d_seg_cstar + step_at(rec_set, slot), 0x7f, sizeof(int), st));
         dev::k_adj_argmin<<<nblk(v.N, 256), 256, 0, st>>>(v.mv, v.d_alpha, v.d_alpha_vis, v.p.equation == 2 ? 1 : 0,
-                                                          v.p.CFL, &v.d_state->dtmin_bits, d_seg_cstar + slot);
+                                                          v.p.CFL, &v.d_state->dtmin_bits, d_seg_cstar + step_at(rec_set, slot));
         dev::launch_dt_final(st, v.d_state, true);
-        AK(cudaMemcpyAsync(d_seg_dt + 2 * slot, &v.d_state->dt, sizeof(double), cudaMemcpyDeviceToDevice, st));
-        AK(cudaMemcpyAsync(d_seg_dt + 2 * slot + 1, &v.d_state->dt_raw, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        AK(cudaMemcpyAsync(d_seg_dt + 2 * step_at(rec_set, slot), &v.d_state->dt, sizeof(double), cudaMemcpyDeviceToDevice, st));
+        AK(cudaMemcpyAsync(d_seg_dt + 2 * step_at(rec_set, slot) + 1, &v.d_state->dt_raw, sizeof(double), cudaMemcpyDeviceToDevice, st));
         // each stage's residual and edge tape go to the segment's buffers (kept for the reverse sweep)
         auto stage = [&](int si, int kind) {
-            v.d_rec_R = seg_R[(size_t)slot * nst + si];
-            v.rec_tape.v = seg_tape[(size_t)slot * nst + si];
-            v.rec_tape.flags = seg_tflags[(size_t)slot * nst + si];
+            v.d_rec_R = seg_R[at(rec_set, slot, si)];
+            v.rec_tape.v = seg_tape[at(rec_set, slot, si)];
+            v.rec_tape.flags = seg_tflags[at(rec_set, slot, si)];
             v.rec_tape.E = v.E;
-            if (!seg_ctape.empty()) v.rec_ctape = seg_ctape[(size_t)slot * nst + si];
+            if (!seg_ctape.empty()) v.rec_ctape = seg_ctape[at(rec_set, slot, si)];
             v.enqueue_stage(kind);
             if (!seg_gx.empty()) {  // the gradients this stage's viscous fluxes read
-                AK(cudaMemcpyAsync(seg_gx[(size_t)slot * nst + si], v.d_Gx, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice,
+                AK(cudaMemcpyAsync(seg_gx[at(rec_set, slot, si)], v.d_Gx, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice,
                                    st));
-                AK(cudaMemcpyAsync(seg_gy[(size_t)slot * nst + si], v.d_Gy, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice,
+                AK(cudaMemcpyAsync(seg_gy[at(rec_set, slot, si)], v.d_Gy, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice,
                                    st));
             }
             return 0;
@@ -685,9 +735,9 @@ struct Adjoint {
         } else {
             const bool kutta = v.p.time_advance == 3103;
             if (int rc = stage(0, kutta ? dev::STAGE_RK3_1 : dev::STAGE_SSP_1)) return rc;
-            AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst + 1], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
+            AK(cudaMemcpyAsync(seg_states[at(rec_set, slot, 1)], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
             if (int rc = stage(1, kutta ? dev::STAGE_RK3_2 : dev::STAGE_SSP_2)) return rc;
-            AK(cudaMemcpyAsync(seg_states[(size_t)slot * nst + 2], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
+            AK(cudaMemcpyAsync(seg_states[at(rec_set, slot, 2)], v.d_U, sizeof(d4) * v.N, cudaMemcpyDeviceToDevice, st));
             if (int rc = stage(2, kutta ? dev::STAGE_RK3_3 : dev::STAGE_SSP_3)) return rc;
         }
         v.d_rec_R = nullptr;
@@ -707,7 +757,7 @@ struct Adjoint {
         if (!seed) seed = d_lam;
         if (!out) out = d_lam_in;
         Solver& v = *s;
-        cudaStream_t st = v.stream;
+        cudaStream_t st = vstream();
         const bool ns = v.p.equation == 2;
         const bool linear = v.p.reconstruct == 3002 || ns;  // the step computes (and reads) gradients
         const int nbE = nblk(v.E, dev::kEdgeThreads), nbN = nblk(v.N, 256);
@@ -745,22 +795,22 @@ struct Adjoint {
     // lam (adjoint of U_{n+1}) -> lam (adjoint of U_n) for the step kept in slot
     int step_vjp(int slot) {
         Solver& v = *s;
-        cudaStream_t st = v.stream;
-        const double* dtp = d_seg_dt + 2 * slot;
+        cudaStream_t st = vstream();
+        const double* dtp = d_seg_dt + 2 * step_at(rev_set, slot);
         const int nbN = nblk(v.N, 256);
-        auto R = [&](int si) { return seg_R[(size_t)slot * nst + si]; };
+        auto R = [&](int si) { return seg_R[at(rev_set, slot, si)]; };
         auto ctp = [&](int si) {
-            return seg_ctape.empty() ? dev::CellTape() : seg_ctape[(size_t)slot * nst + si];
+            return seg_ctape.empty() ? dev::CellTape() : seg_ctape[at(rev_set, slot, si)];
         };
         // the stage's recorded gradients for the viscous reverse (Navier-Stokes)
         auto use = [&](int si) {
-            vis_gx = seg_gx.empty() ? nullptr : seg_gx[(size_t)slot * nst + si];
-            vis_gy = seg_gy.empty() ? nullptr : seg_gy[(size_t)slot * nst + si];
+            vis_gx = seg_gx.empty() ? nullptr : seg_gx[at(rev_set, slot, si)];
+            vis_gy = seg_gy.empty() ? nullptr : seg_gy[at(rev_set, slot, si)];
         };
         auto tp = [&](int si) {
             dev::EdgeTape t;
-            t.v = seg_tape[(size_t)slot * nst + si];
-            t.flags = seg_tflags[(size_t)slot * nst + si];
+            t.v = seg_tape[at(rev_set, slot, si)];
+            t.flags = seg_tflags[at(rev_set, slot, si)];
             t.E = v.E;
             return t;
         };
@@ -769,7 +819,7 @@ struct Adjoint {
         if (v.p.time_advance == 3101) {
             // U1 = U0 + dt R(U0): a = 0, b = 1
             use(0);
-            if ((rc = stage_vjp(seg_states[(size_t)slot], tp(0), ctp(0), R(0), dtp, 0.0, 1.0, 2, 0))) return rc;
+            if ((rc = stage_vjp(seg_states[at(rev_set, slot, 0)], tp(0), ctp(0), R(0), dtp, 0.0, 1.0, 2, 0))) return rc;
             std::swap(d_lam, d_lam_in);
         } else if (v.p.time_advance == 3103) {
             // Kutta RK3: k1 = R(U0), U1 = U0 + dt/2 k1; k2 = R(U1), U2 = U0 - dt k1 + 2 dt k2;
@@ -778,9 +828,9 @@ struct Adjoint {
             //   s3 = L3/6,  s2 = 2/3 L3 + 2 L2,  s1 = L3/6 - L2 + L1/2,
             // L2 = dt J2^T s3 and L1 = dt J1^T s2 being the adjoints of U2 and U1, and
             //   lam_U0 = L3 + L2 + L1 + dt J0^T s1;  d loss / d dt = s3.k3 + s2.k2 + s1.k1.
-            const d4* U0 = seg_states[(size_t)slot * 3];
-            const d4* U1 = seg_states[(size_t)slot * 3 + 1];
-            const d4* U2 = seg_states[(size_t)slot * 3 + 2];
+            const d4* U0 = seg_states[at(rev_set, slot, 0)];
+            const d4* U1 = seg_states[at(rev_set, slot, 1)];
+            const d4* U2 = seg_states[at(rev_set, slot, 2)];
             const int nbk = nblk(v.N, 256);
             // L2 = dt J2^T (L3/6): seed L3, b = 1/6, no identity term
             use(2);
@@ -801,9 +851,9 @@ struct Adjoint {
             b1 = 1.0;
             b2 = 1.0;
         } else {
-            const d4* U0 = seg_states[(size_t)slot * 3];
-            const d4* U1 = seg_states[(size_t)slot * 3 + 1];
-            const d4* U2 = seg_states[(size_t)slot * 3 + 2];
+            const d4* U0 = seg_states[at(rev_set, slot, 0)];
+            const d4* U1 = seg_states[at(rev_set, slot, 1)];
+            const d4* U2 = seg_states[at(rev_set, slot, 2)];
             // U3 = 1/3 U0 + 2/3 (U2 + dt R(U2))
             use(2);
             if ((rc = stage_vjp(U2, tp(2), ctp(2), R(2), dtp, 1.0 / 3.0, 2.0 / 3.0, 0, 0))) return rc;
@@ -820,8 +870,8 @@ struct Adjoint {
             b1 = 0.25;
             b2 = 1.0;
         }
-        dev::k_adj_dt<<<1, dev::kDtThreads, 0, st>>>(d_dotp, nbN, nst, b0, b1, b2, seg_states[(size_t)slot * nst],
-                                                    v.mv, v.gas, v.p.CFL, d_seg_cstar + slot, dtp, d_lam,
+        dev::k_adj_dt<<<1, dev::kDtThreads, 0, st>>>(d_dotp, nbN, nst, b0, b1, b2, seg_states[at(rev_set, slot, 0)],
+                                                    v.mv, v.gas, v.p.CFL, d_seg_cstar + step_at(rev_set, slot), dtp, d_lam,
                                                     v.p.equation == 2 ? 1 : 0,
                                                     std::max(4.0 / 3.0, v.p.gamma / v.p.Pr));
         AK(cudaGetLastError());
@@ -886,13 +936,17 @@ struct Adjoint {
         return 0;
     }
 
-    // segment work of the reverse sweep for a segment of n steps (see SegGraph): recomputes
-    // the segment's steps kernel by kernel when rec (its checkpoint already loaded), then runs
-    // the VJPs of its steps from the last to the first
-    int run_segment(int n, bool rec) {
+    // segment work of the reverse sweep (see SegGraph): records nrec steps of a segment into
+    // set rec_set (its checkpoint already loaded) and reverses the n steps held in set rev_set.
+    // Sequential: the recording first, then the reverse, on the solver's stream (the same
+    // segment, rec_set == rev_set).  Overlap: the reverse of one segment on rstream beside the
+    // recording of the one before it on the solver's stream (rec_set != rev_set), forked and
+    // joined with events inside the captured graph.
+    int run_graph(int n, int nrec, bool overlap) {
         Solver& v = *s;
         for (const SegGraph& g : seg_graphs)
-            if (g.n == n && g.rec == rec && g.lam0 == d_lam) {
+            if (g.n == n && g.nrec == nrec && g.overlap == overlap && g.rev == rev_set && g.rec == rec_set &&
+                g.lam0 == d_lam) {
                 AK(cudaGraphLaunch(g.exec, v.stream));
                 d_lam = g.lam_out;
                 d_lam_in = g.lam_in_out;
@@ -901,29 +955,53 @@ struct Adjoint {
             }
         SegGraph g;
         g.n = n;
-        g.rec = rec;
+        g.nrec = nrec;
+        g.overlap = overlap;
+        g.rev = rev_set;
+        g.rec = rec_set;
         g.lam0 = d_lam;
         d4* const lam_in0 = d_lam_in;
         const long long before = v.launches;
         AK(cudaStreamBeginCapture(v.stream, cudaStreamCaptureModeThreadLocal));
         int rc = 0;
-        if (rec)
-            for (int k = 0; k < n && !rc; k++) rc = record_step(k);
-        for (int k = n - 1; k >= 0 && !rc; k--) rc = step_vjp(k);
+        cudaError_t ce = cudaSuccess;
+        if (overlap) {
+            ce = cudaEventRecord(ev_fork, v.stream);
+            if (ce == cudaSuccess) ce = cudaStreamWaitEvent(rstream, ev_fork, 0);
+            if (ce == cudaSuccess) vjp_stream = rstream;
+        }
+        if (ce == cudaSuccess) {
+            for (int k = 0; k < nrec && !rc; k++) rc = record_step(k);
+            for (int k = n - 1; k >= 0 && !rc; k--) rc = step_vjp(k);
+        }
+        if (vjp_stream) {  // join the reverse branch whatever happened, so that the capture can end
+            vjp_stream = nullptr;
+            const cudaError_t c1 = cudaEventRecord(ev_join, rstream);
+            const cudaError_t c2 = c1 == cudaSuccess ? cudaStreamWaitEvent(v.stream, ev_join, 0) : c1;
+            if (ce == cudaSuccess) ce = c2;
+        }
         cudaGraph_t graph = nullptr;
         const cudaError_t e = cudaStreamEndCapture(v.stream, &graph);
-        if (rc || e != cudaSuccess) {
+        if (rc || ce != cudaSuccess || e != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
             d_lam = g.lam0;
             d_lam_in = lam_in0;
             v.launches = before;
-            return rc ? rc : fail(FVGB_ERR_CUDA, std::string("adjoint graph capture: ") + cudaGetErrorString(e));
+            if (rc) return rc;
+            return fail(FVGB_ERR_CUDA, std::string("adjoint graph capture: ") +
+                                           cudaGetErrorString(ce != cudaSuccess ? ce : e));
         }
         g.launches = v.launches - before;
         v.launches = before;
         g.lam_out = d_lam;
         g.lam_in_out = d_lam_in;
-        const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+        // the kernels keep the priorities of the streams they were captured from: the reverse
+        // branch, the longer of the two, goes first where both have blocks waiting
+        cudaError_t ei = cudaGraphInstantiateWithFlags(&g.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+        if (ei != cudaSuccess) {
+            (void)cudaGetLastError();
+            ei = cudaGraphInstantiate(&g.exec, graph, 0);
+        }
         cudaGraphDestroy(graph);
         if (ei != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("adjoint graph instantiate: ") + cudaGetErrorString(ei));
         seg_graphs.push_back(g);
@@ -953,8 +1031,9 @@ struct Adjoint {
             const int n = std::min(S, K - i * S);
             if (i + 1 < nseg) {
                 if ((rc = v.step_async(v.p.T_end, n))) return rc;
-            } else if ((rc = record_segment(i))) {  // the reverse sweep starts here: keep its states now
-                return rc;
+            } else {  // the reverse sweep starts here: keep its states now, in set 0
+                rec_set = 0;
+                if ((rc = record_segment(i))) return rc;
             }
         }
         AK(cudaEventRecord(b, v.stream));
@@ -987,14 +1066,39 @@ struct Adjoint {
         AK(cudaEventCreate(&a));
         AK(cudaEventCreate(&b));
         AK(cudaEventRecord(a, st));
-        for (int i = nseg - 1; i >= 0; i--) {
-            // the last segment's states are still those the forward sweep recorded
-            const bool rec = i + 1 < nseg || !last_kept;
-            if (rec) {
-                if ((rc = load_segment(i))) return rc;
+        if (nsets == 2) {
+            // segment i's records in set cur; the one before it recorded into the other set
+            // beside its reverse.  The last segment's records are still those the forward sweep
+            // kept in set 0, unless a backward sweep has used the sets since.
+            int cur = 0;
+            if (!last_kept) {
+                rec_set = rev_set = 0;
+                if ((rc = load_segment(nseg - 1))) return rc;
                 AK(cudaMemcpyAsync(&v.d_state->T, &v.p.T_end, sizeof(double), cudaMemcpyHostToDevice, st));
+                if ((rc = run_graph(0, seg_len(nseg - 1), false))) return rc;
             }
-            if ((rc = run_segment(std::min(S, K - i * S), rec))) return rc;
+            for (int i = nseg - 1; i >= 0; i--) {
+                rev_set = cur;
+                rec_set = 1 - cur;
+                const int nrec = i > 0 ? seg_len(i - 1) : 0;
+                if (nrec) {
+                    if ((rc = load_segment(i - 1))) return rc;
+                    AK(cudaMemcpyAsync(&v.d_state->T, &v.p.T_end, sizeof(double), cudaMemcpyHostToDevice, st));
+                }
+                if ((rc = run_graph(seg_len(i), nrec, nrec > 0))) return rc;
+                cur = 1 - cur;
+            }
+        } else {
+            rec_set = rev_set = 0;
+            for (int i = nseg - 1; i >= 0; i--) {
+                // the last segment's states are still those the forward sweep recorded
+                const bool rec = i + 1 < nseg || !last_kept;
+                if (rec) {
+                    if ((rc = load_segment(i))) return rc;
+                    AK(cudaMemcpyAsync(&v.d_state->T, &v.p.T_end, sizeof(double), cudaMemcpyHostToDevice, st));
+                }
+                if ((rc = run_graph(seg_len(i), rec ? seg_len(i) : 0, false))) return rc;
+            }
         }
         last_kept = nseg == 1;
         AK(cudaEventRecord(b, st));
@@ -1085,6 +1189,16 @@ extern "C" int fvgb_adjoint_backward(fvgb_handle* h, const double* seed_UK, doub
     int rc = a->adj.backward(seed_UK, grad_U0);
     if (ms_backward) *ms_backward = a->adj.ms_bwd;
     return rc;
+}
+
+extern "C" int fvgb_adjoint_overlap(fvgb_handle* h, int mode, int* overlapped) {
+    if (!h || (mode != 0 && mode != 1)) return fail(FVGB_ERR_ARG, "fvgb_adjoint_overlap: mode is 0 or 1");
+    h->s.adj_overlap = mode;
+    if (overlapped) {
+        AdjHandle* a = find_adj(h);
+        *overlapped = a && a->adj.nsets == 2 ? 1 : 0;
+    }
+    return 0;
 }
 
 extern "C" void fvgb_adjoint_release(fvgb_handle* h) {

@@ -30,6 +30,7 @@ struct Solver {
     dev::MeshView mv{};
     long long launches = 0, launches_per_step = 0;
     dev::Status seen{};
+    int adj_overlap = 1;  // fvgb_adjoint_overlap: recompute beside the reverse sweep where memory allows
 
     // layout
     int *d_e_L = nullptr, *d_e_R = nullptr, *d_e_bc = nullptr;

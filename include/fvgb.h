@@ -298,6 +298,14 @@ int fvgb_adjoint_forward(fvgb_handle* h, int nsteps, int n_checkpoints, const do
                          double* ms_forward);
 int fvgb_adjoint_backward(fvgb_handle* h, const double* seed_UK, double* grad_U0, double* ms_backward);
 void fvgb_adjoint_release(fvgb_handle* h);
+/* mode 1 (the default): fvgb_adjoint_forward lays out a second set of segment
+ * records where the device has room for it and 1 GiB besides, and the backward
+ * sweep recomputes each segment on the handle's stream beside the reverse of the
+ * segment after it on a second stream.  Mode 0: one set, recomputation and
+ * reverse one after the other.  The gradient is bitwise the same.  Takes effect
+ * at the next fvgb_adjoint_forward; *overlapped (may be null) reports whether
+ * the current adjoint workspace has the second set. */
+int fvgb_adjoint_overlap(fvgb_handle* h, int mode, int* overlapped);
 /* The residual's vector-Jacobian product grad_U = (dR/dU)^T seed_R at the state U,
  * where R is what fvgb_rhs returns for U (calculateFunctionF, FVMR/src/time/
  * Evolve.cpp:98-112): the reverse of the edge fluxes with their boundary ghosts,

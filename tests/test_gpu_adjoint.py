@@ -120,6 +120,42 @@ def test_checkpoints_do_not_change_the_gradient(tmp_path):
     assert np.array_equal(grads[0], grads[1]) and np.array_equal(grads[1], grads[2])
 
 
+@pytest.mark.parametrize("kind", ["ssp_lsq_barth", "kutta_gg", "euler_o1", "ns_vortex"])
+def test_overlapped_sweep_is_bitwise_the_sequential_one(tmp_path, kind):
+    """The backward sweep with each segment's recomputation on the solver's stream beside the
+    reverse of the next segment (two sets of records, one graph with two branches) against the
+    sweep that recomputes and reverses one after the other: the same kernels on the same data,
+    so the gradient is bitwise equal.  Seven steps in segments of 3, 3 and 1; a second backward
+    after the first (the forward's last segment no longer kept) gives the same gradient."""
+    from cfd_solver_2d_gpu_gb300 import adjoint_overlap
+    if kind == "ns_vortex":
+        su2 = cases.square_mesh(16, jitter=0.2, directory=str(tmp_path))
+        text = cases.toml_text(equation=2, flux=2002, reconstruct=3002, gradient=1, limiter=1, time_advance=3104,
+                               CFL=0.6, Re=100.0)
+        p, solver, U0, Ut0 = boundary_case(tmp_path, kind, text, su2)
+    else:
+        ta, rc, gr, lim = {"ssp_lsq_barth": (3104, 3002, 1, 1), "kutta_gg": (3103, 3002, 2, 1),
+                           "euler_o1": (3101, 3001, 1, 0)}[kind]
+        tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=16, time_advance=ta, reconstruct=rc, gradient=gr,
+                                                       limiter=lim)
+    K = 7
+    rho_t = forward(solver, p, Ut0, K)[0]
+    out = {}
+    for mode in (1, 0):
+        adjoint_overlap(solver, mode)
+        UK, _ = adjoint_forward(solver, U0, K, 3)
+        assert adjoint_overlap(solver) == bool(mode)
+        _, seed = loss_seed(UK, rho_t)
+        g1, _ = adjoint_backward(solver, seed)
+        g2, _ = adjoint_backward(solver, seed)
+        assert np.all(np.isfinite(g1))
+        assert np.array_equal(g1, g2)
+        out[mode] = (UK, g1)
+    adjoint_overlap(solver, 1)
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+
+
 def test_against_oracle_finite_differences(tmp_path):
     """The reference gradient: central differences of the oracle's forward map (CPU)."""
     tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=12)
