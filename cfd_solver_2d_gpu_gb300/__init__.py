@@ -104,6 +104,7 @@ def lib():
             "fvgb_step": (i, [v, dp, d, i]),
             "fvgb_step_async": (i, [v, d, i]),
             "fvgb_set_time": (i, [v, d]),
+            "fvgb_set_cfl": (i, [v, d]),
             "fvgb_time": (i, [v, dp, dp]),
             "fvgb_synchronize": (i, [v]),
             "fvgb_rhs": (i, [v, dp, dp, dp, dp]),
@@ -332,6 +333,9 @@ class GPUSolver2:
 
     def set_time(self, t):
         _check(lib().fvgb_set_time(self._h, float(t)))
+
+    def set_cfl(self, CFL):
+        _check(lib().fvgb_set_cfl(self._h, float(CFL)))
 
     def time(self):
         t, dt = ctypes.c_double(), ctypes.c_double()

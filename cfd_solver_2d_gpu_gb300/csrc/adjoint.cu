@@ -520,6 +520,13 @@ struct Adjoint {
     cudaStream_t rstream = nullptr;     // the reverse sweep's stream beside a recomputation
     cudaStream_t vjp_stream = nullptr;  // where the VJPs are enqueued (null: the solver's stream)
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // what the workspace was laid out for: a forward with the same steps, checkpoints, overlap
+    // mode and CFL (captured by value in the graphs) reuses it, graphs included
+    int req_ncheck = 0, req_overlap = 0;
+    double req_cfl = 0.0;
+    bool reusable(int nsteps, int ncheck) const {
+        return K == nsteps && req_ncheck == ncheck && req_overlap == s->adj_overlap && req_cfl == s->p.CFL;
+    }
     size_t at(int set, int slot, int si) const { return ((size_t)set * S + slot) * nst + si; }
     size_t step_at(int set, int slot) const { return (size_t)set * S + slot; }
     cudaStream_t vstream() const { return vjp_stream ? vjp_stream : s->stream; }
@@ -601,6 +608,9 @@ struct Adjoint {
                 return fail(FVGB_ERR_UNSUPPORTED, "unknown boundary type");
         }
         K = nsteps;
+        req_ncheck = ncheck;
+        req_overlap = s->adj_overlap;
+        req_cfl = p.CFL;
         ncheck = std::max(1, std::min(ncheck, K));
         S = (K + ncheck - 1) / ncheck;
         nseg = (K + S - 1) / S;
@@ -1168,15 +1178,25 @@ extern "C" int fvgb_adjoint_forward(fvgb_handle* h, int nsteps, int n_checkpoint
                                     double* U_K, double* ms_forward) {
     if (!h || !U0 || nsteps <= 0) return fail(FVGB_ERR_ARG, "bad adjoint arguments");
     cudaSetDevice(h->s.p.device);
-    drop_adj(h, g_adj);
-    AdjHandle* a = new AdjHandle{h, Adjoint()};
-    int rc = a->adj.setup(&h->s, nsteps, n_checkpoints);
+    // the workspace of the previous forward serves again when laid out for the same run
+    AdjHandle* a = find_adj(h);
+    if (a && !a->adj.reusable(nsteps, n_checkpoints)) {
+        drop_adj(h, g_adj);
+        a = nullptr;
+    }
+    const bool fresh = a == nullptr;
+    int rc = 0;
+    if (fresh) {
+        a = new AdjHandle{h, Adjoint()};
+        rc = a->adj.setup(&h->s, nsteps, n_checkpoints);
+    }
     if (!rc) rc = a->adj.forward(U0, t0, U_K);
     if (rc) {
-        delete a;
+        if (fresh) delete a;
+        else drop_adj(h, g_adj);
         return rc;
     }
-    add_adj(a, g_adj);
+    if (fresh) add_adj(a, g_adj);
     if (ms_forward) *ms_forward = a->adj.ms_fwd;
     return 0;
 }

@@ -293,7 +293,10 @@ int fvgb_output_timed(fvgb_handle* h, int reps, double* ms_node_field, double* m
  * returns U_K; fvgb_adjoint_backward then maps a seed dL/dU_K to dL/dU_0
  * (both [4][N], reference numbering), recomputing each segment once.  The
  * handle's state afterwards is U_K.  Fails with FVGB_ERR_UNSUPPORTED outside
- * that scope, and when the positivity pass acted during the run. */
+ * that scope, and when the positivity pass acted during the run.  A forward
+ * with the same nsteps, n_checkpoints, overlap mode and CFL as the handle's
+ * previous one reuses its workspace: the device buffers and the backward
+ * sweep's captured graphs. */
 int fvgb_adjoint_forward(fvgb_handle* h, int nsteps, int n_checkpoints, const double* U0, double t0, double* U_K,
                          double* ms_forward);
 int fvgb_adjoint_backward(fvgb_handle* h, const double* seed_UK, double* grad_U0, double* ms_backward);

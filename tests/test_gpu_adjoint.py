@@ -156,6 +156,37 @@ def test_overlapped_sweep_is_bitwise_the_sequential_one(tmp_path, kind):
     assert np.array_equal(out[0][1], out[1][1])
 
 
+def test_workspace_reuse(tmp_path):
+    """A forward with the same steps, checkpoints, overlap mode and CFL reuses the previous
+    forward's workspace and the backward sweep's captured graphs: the gradients equal those of
+    a fresh workspace bitwise, for other initial states and seeds, and after a CFL change (which
+    lays the workspace out again)."""
+    tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=16)
+    K, nck = 7, 3
+    rng = np.random.default_rng(12)
+    U0b = U0 * (1 + 1e-3 * rng.standard_normal(U0.shape))
+    seed_a, seed_b = rng.standard_normal(U0.shape), rng.standard_normal(U0.shape)
+
+    def run(U, seed, fresh):
+        if fresh:
+            fv.lib().fvgb_adjoint_release(solver._h)
+        UK, _ = adjoint_forward(solver, U, K, nck)
+        return UK, adjoint_backward(solver, seed)[0]
+
+    a1 = run(U0, seed_a, True)
+    b_reused = run(U0b, seed_b, False)
+    a_reused = run(U0, seed_a, False)
+    b_fresh = run(U0b, seed_b, True)
+    for x, y in ((a1, a_reused), (b_reused, b_fresh)):
+        assert np.array_equal(x[0], y[0]) and np.array_equal(x[1], y[1])
+    assert not np.array_equal(a1[1], b_fresh[1])
+    solver.set_cfl(0.6)
+    c_after = run(U0, seed_a, False)
+    c_fresh = run(U0, seed_a, True)
+    assert np.array_equal(c_after[1], c_fresh[1])
+    assert not np.array_equal(c_after[1], a1[1])
+
+
 def test_against_oracle_finite_differences(tmp_path):
     """The reference gradient: central differences of the oracle's forward map (CPU)."""
     tp, su2, p, mesh, solver, U0, Ut0 = setup_case(tmp_path, n=12)
