@@ -17,8 +17,8 @@
 // extra forward pass and about K/S 4N + S (74 N + 117 E) doubles (sqrt(K)
 // checkpoints: O(sqrt(K) N)).  Where the device has room for a second set of segment
 // records (and fvgb_adjoint_overlap has not turned it off), the recomputation of segment
-// i-1 runs on the solver's stream beside the reverse sweep of segment i on a second,
-// higher-priority stream: both are branches of one CUDA graph, and the two sets of records
+// i-1 runs on the solver's stream beside the reverse sweep of segment i on a second
+// stream: both are branches of one CUDA graph, and the two sets of records
 // alternate.  The kernels and their inputs are the same either way, so the gradient is
 // bitwise the same; the small per-stage kernels of a 10^5-cell mesh leave enough of the
 // SMs idle for the two sweeps to share them.
@@ -662,9 +662,7 @@ struct Adjoint {
             const size_t used = free0 > free1 ? free0 - free1 : 0;
             if (free1 > used + ((size_t)1 << 30)) {  // room for a second set and 1 GiB besides
                 if ((rc = alloc_set(1))) return rc;
-                int least = 0, greatest = 0;
-                AK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-                AK(cudaStreamCreateWithPriority(&rstream, cudaStreamNonBlocking, greatest));
+                AK(cudaStreamCreateWithFlags(&rstream, cudaStreamNonBlocking));
                 AK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
                 AK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
                 nsets = 2;
@@ -1005,13 +1003,11 @@ struct Adjoint {
         v.launches = before;
         g.lam_out = d_lam;
         g.lam_in_out = d_lam_in;
-        // the kernels keep the priorities of the streams they were captured from: the reverse
-        // branch, the longer of the two, goes first where both have blocks waiting
-        cudaError_t ei = cudaGraphInstantiateWithFlags(&g.exec, graph, cudaGraphInstantiateFlagUseNodePriority);
-        if (ei != cudaSuccess) {
-            (void)cudaGetLastError();
-            ei = cudaGraphInstantiate(&g.exec, graph, 0);
-        }
+        // no node priorities: with the reverse branch first wherever both branches had blocks
+        // waiting (cudaGraphInstantiateFlagUseNodePriority, the reverse captured from a stream
+        // of the highest priority) the 500-step sweep of the 256x256 mesh took 285 ms, without
+        // them 276 ms
+        const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
         cudaGraphDestroy(graph);
         if (ei != cudaSuccess) return fail(FVGB_ERR_CUDA, std::string("adjoint graph instantiate: ") + cudaGetErrorString(ei));
         seg_graphs.push_back(g);
